@@ -1,0 +1,435 @@
+#!/usr/bin/env python3
+"""bench.py -- chain-steps/s of the RFMF annealer on GB300.
+
+Workload (the plain-method mid-size configuration): a 50x60 toroidal grid
+(n=3000, 6000 edges, weights uniform +-1) and an Erdos-Renyi graph n=2000
+with mean degree ~19 (weights uniform +-1), 1024 chains per graph (raw seeds
+0..1023 per graph on rank 0), the reference's default schedule (phases
+128,64,32,16,8,4,2,1 with equal sweeps per phase) and t0 ladder
+35,50,70,100,140,200,280,400 assigned round-robin.  Synthetic seeded graphs
+of those shapes stand in for the Gset instances.
+
+One STEP is one persistent launch that advances all 2048 chains by
+sweeps/steps sweeps; the K timed steps together are one complete anneal of
+--sweeps sweeps per chain (default 10^7, the configuration's budget), with the
+chain state resident on the device between steps.  value = chains * sweeps /
+(sum of the K launch times, CUDA events on the library's stream).  The L2 is
+flushed (256 MB write) between timed steps, outside the events.
+
+e2e: the same metric through the public drop-in call (rfmf_graph_create +
+rfmf_anneal, host buffers, synchronous) on the same graphs and chains with
+sweeps/steps sweeps per chain per call, host<->device copies inside the
+timed region.
+
+--impl reference: the CPU restatement of the reference's sweep (oracle/,
+there is no CPU annealer in the reference) on all host cores, on a bounded
+sample of the same workload.
+"""
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+LADDER = [35.0, 50.0, 70.0, 100.0, 140.0, 200.0, 280.0, 400.0]
+PHASES = [128, 64, 32, 16, 8, 4, 2, 1]
+WORKLOAD = "torus50x60_pm1+er2000_d19_pm1"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def workload_graphs():
+    import rfmf_gb300 as R
+    return [R.torus(50, 60, signed=True, seed=0, name="torus50x60"),
+            R.erdos_renyi_degree(2000, 19, signed=True, seed=0, name="er2000_d19")]
+
+
+def chain_setup(graphs, chains_per_graph, seed_base):
+    import rfmf_gb300 as R
+    per = []
+    for g in graphs:
+        seeds = [seed_base + i for i in range(chains_per_graph)]
+        per.append(dict(g=g, seeds=seeds,
+                        init=np.stack([R.initial_spins(s, g.n) for s in seeds]),
+                        solver=[R.solver_seed(s) for s in seeds],
+                        t0s=[LADDER[i % 8] for i in range(chains_per_graph)]))
+    return per
+
+
+def schedule(sweeps):
+    per = sweeps // len(PHASES)
+    return PHASES, [per] * len(PHASES)
+
+
+def sweep_bytes(n, m, P):
+    """Algorithmic bytes of one chain-sweep (excluding best-spin copies):
+    SELECT reads spin (1 B) + local field (4 B) per vertex; FLIP per winner
+    reads an offsets pair (8 B), walks its row (8 B/entry) and updates each
+    neighbour's field (8 B/entry)."""
+    Pe = min(P, n)
+    dbar = 2.0 * m / n
+    return 5.0 * n + Pe * (8.0 + 16.0 * dbar)
+
+
+def window_bytes(graphs_chains, phases, iters, s0, s1):
+    """Sum of sweep_bytes over executed sweeps [s0, s1) for every chain."""
+    tot = 0.0
+    for g, nch in graphs_chains:
+        acc = 0
+        for P, it in zip(phases, iters):
+            if P == 0:
+                continue
+            lo, hi = max(s0, acc), min(s1, acc + it)
+            if hi > lo:
+                tot += nch * (hi - lo) * sweep_bytes(g.n, g.m, P)
+            acc += it
+    return tot
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(", ") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].strip() == "Active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        load = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            return {}
+    return {}
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the annealing kernel from a committed ncu
+    summary (profiles/anneal_kernel_traffic.json), or None."""
+    p = ROOT / "profiles" / "anneal_kernel_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            return None
+    return None
+
+
+# --------------------------------------------------------------- CPU arms
+def cpu_rate(graphs, steps, warmup, target_s, rank_seed_base=0):
+    """Oracle on all host cores: one chain per core over a compressed schedule
+    (same phases, equal sweeps per phase) on the workload's graphs."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as ora
+    import rfmf_gb300 as R
+    ora.lib()
+    cores = ora.default_threads()
+    # calibrate sweeps so one step takes ~target_s
+    g0 = graphs[0]
+    t = time.perf_counter()
+    ora.anneal(g0, R.initial_spins(1, g0.n)[None], [35.0], [R.solver_seed(1)], PHASES, [40] * 8,
+               nthreads=1)
+    per_sweep = (time.perf_counter() - t) / 320 * (sum(g.n for g in graphs) / g0.n / len(graphs))
+    sweeps = max(800, int(target_s / max(per_sweep, 1e-7) / 8) * 8)
+    nch = max(cores, 2)
+    per_graph = [nch // 2, nch - nch // 2]
+    rates = []
+    for step in range(warmup + steps):
+        total_chain_sweeps = 0
+        t = time.perf_counter()
+        for g, k in zip(graphs, per_graph):
+            seeds = [rank_seed_base + 10000 * step + i for i in range(k)]
+            init = np.stack([R.initial_spins(s, g.n) for s in seeds])
+            ora.anneal(g, init, [LADDER[i % 8] for i in range(k)],
+                       [R.solver_seed(s) for s in seeds], PHASES, [sweeps // 8] * 8,
+                       nthreads=cores)
+            total_chain_sweeps += k * sweeps
+        el = time.perf_counter() - t
+        if step >= warmup:
+            rates.append((total_chain_sweeps, el))
+    cs = sum(r[0] for r in rates)
+    el = sum(r[1] for r in rates)
+    sample = (f"{per_graph[0]}+{per_graph[1]} chains (torus50x60 + er2000_d19) x {sweeps} sweeps "
+              f"(phases 128..1, {sweeps // 8} each) per step, {steps} step(s)")
+    return cs / el, cores, sample, el
+
+
+# --------------------------------------------------------------- GPU arm
+def gpu_arm(args, rank, world):
+    import torch
+
+    import rfmf_gb300 as R
+    R.lib(build_if_missing=True)
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    ctx = R.Context(dev)
+    graphs = workload_graphs()
+    dgs = [R.DeviceGraph(ctx, g) for g in graphs]
+    K, W = args.steps, args.warmup
+    sweeps = args.sweeps
+    if sweeps % (8 * K):
+        sweeps = (sweeps // (8 * K)) * 8 * K
+    per_step = sweeps // K
+    phases, iters = schedule(sweeps)
+    cfg = R.make_config(threads_per_chain=args.threads, reg_variant=args.variant)
+    base = rank * args.chains
+    setup = chain_setup(graphs, args.chains, base)
+
+    def batch_for(setup_, ph, it):
+        gl, ini, sol, t0 = [], [], [], []
+        for k, s in enumerate(setup_):
+            gl += [dgs[k]] * len(s["seeds"])
+            ini += list(s["init"])
+            sol += s["solver"]
+            t0 += s["t0s"]
+        return R.Batch(ctx, gl, t0, sol, ini, ph, it, cfg)
+
+    # warm-up: W launches of a separate anneal (different seeds), same sizes
+    wsetup = chain_setup(graphs, args.chains, base + 1_000_000)
+    wb = batch_for(wsetup, phases, iters)
+    for _ in range(W):
+        wb.run_timed(per_step)
+    info = wb.info()
+    wb.close()
+
+    b = batch_for(setup, phases, iters)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    gc = [(g, args.chains) for g in graphs]
+    clocks = ClockSampler(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_wall = time.perf_counter()
+    step_ms, step_bytes = [], []
+    imp_prev = np.zeros(len(graphs) * args.chains, np.uint64)
+    for k in range(K):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ms = b.run_timed(per_step)
+        step_ms.append(ms)
+        imp = b.improved_sweeps()
+        d_imp = (imp - imp_prev).astype(np.float64)
+        imp_prev = imp
+        ns = np.concatenate([[g.n] * args.chains for g in graphs])
+        step_bytes.append(window_bytes(gc, phases, iters, k * per_step, (k + 1) * per_step) +
+                          float(np.dot(ns, d_imp)))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    total_ms = sum(step_ms)
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    out = b.read()
+    done = out["sweeps_done"]
+    assert all(int(d) == sweeps for d in done), "not every chain finished its schedule"
+    chain_steps = len(graphs) * args.chains * sweeps
+    value = chain_steps * world / (total_ms / 1e3)
+    # consistency: kernel-tracked best == recompute of best spins (spot check)
+    for i in (0, args.chains):
+        g = graphs[i // args.chains]
+        assert out["best_vals"][i] == g.cut_value(out["best_spins"][i])
+    b.close()
+
+    # e2e through the drop-in call with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_arm(args, ctx, graphs, setup, per_step)
+
+    peaks = measured_peaks()
+    sm_count = ctx.info()["sm_count"]
+    sm_mhz = clk["sm_mhz"] or peaks.get("sm_max_mhz", 2070.0)
+    smem_peak = sm_count * 128.0 * sm_mhz * 1e6 / 1e9   # GB/s
+    achieved = sum(step_bytes) / (total_ms / 1e3) / 1e9
+    traffic = profile_traffic()
+    result = {
+        "metric": "chain-steps/s",
+        "value": value,
+        "unit": "chain-steps/s",
+        "n_gpus": world,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": total_ms / K,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int32",
+        "data": "synthetic (seeded torus 50x60 +-1 and Erdos-Renyi n=2000 d~19 +-1)",
+        "config": {
+            "workload": WORKLOAD,
+            "graphs": [dict(name=g.name, n=g.n, m=g.m, B=g.max_weighted_degree()) for g in graphs],
+            "chains_per_graph": args.chains,
+            "sweeps_per_chain": sweeps,
+            "sweeps_per_step": per_step,
+            "phases": PHASES,
+            "t0_ladder": LADDER,
+            "threads_per_chain": info["threads_per_chain"],
+            "reg_variant": info["reg_variant"],
+            "grid": info["grid"],
+            "score_path": "int64" if info["score64"] else "int32",
+            "l2": "flushed (256 MB write) between timed steps",
+            "parallelism": f"replicas x{world}",
+        },
+        "gpu_launches": K,
+        "e2e": e2e,
+        "clocks": clk,
+        "roofline": {
+            "bound": "smem",
+            "achieved": achieved,
+            "peak": smem_peak,
+            "unit": "GB/s",
+            "frac": achieved / smem_peak,
+            "traffic": (traffic or {}).get("dram_bytes_per_launch_scaled"),
+            "peak_source": f"{sm_count} SMs x 128 B/clk x {sm_mhz:.0f} MHz (median SM clock sampled "
+                           "during the timed region)",
+            "bytes_model": "5n + min(P,n)(8 + 16 dbar) per chain-sweep + n per improving sweep",
+        },
+        "wall_s": wall,
+    }
+    return result
+
+
+def e2e_arm(args, ctx, graphs, setup, per_step):
+    import rfmf_gb300 as R
+    phases, iters = schedule(per_step)
+    K = args.steps
+    h2d = d2h = 0
+    t = time.perf_counter()
+    for _ in range(K):
+        for s in setup:
+            g = s["g"]
+            dg = R.DeviceGraph(ctx, g)
+            res = R.anneal_gpu(ctx, dg, g.max_weighted_degree(), s["init"], s["t0s"], phases,
+                               iters, s["solver"])
+            dg.close()
+            C = len(s["seeds"])
+            words = (g.n + 31) // 32
+            runs = len(R.beta_tables(sorted(set(s["t0s"])), per_step)[0])
+            h2d += ((g.n + 1) * 4 + 2 * g.m * 8 + 2 * C * words * 4 + C * (96 + 4) + runs * 12 +
+                    len(phases) * 12)
+            d2h += 2 * C * words * 4 + C * 96
+            assert res.best_vals[0] == g.cut_value(res.best_spins[0])
+    el = time.perf_counter() - t
+    chain_steps = K * sum(len(s["seeds"]) for s in setup) * per_step
+    return {"value": chain_steps / el, "unit": "chain-steps/s",
+            "h2d_bytes_per_step": h2d // K, "d2h_bytes_per_step": d2h // K,
+            "api": "rfmf_graph_create + rfmf_anneal (annealGpu drop-in), host buffers, "
+                   f"{per_step} sweeps per chain per call"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--sweeps", type=int, default=10_000_000)
+    ap.add_argument("--chains", type=int, default=1024)
+    ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--variant", type=int, default=0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        graphs = workload_graphs()
+        per_step_s = max(2.0, 150.0 / max(args.steps + args.warmup, 1))
+        rate, cores, sample, el = cpu_rate(graphs, args.steps, args.warmup, per_step_s)
+        line = {
+            "impl": "reference", "metric": "chain-steps/s", "value": rate,
+            "unit": "chain-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int64", "data": "synthetic", "config": {"workload": WORKLOAD},
+            "cpu_baseline": {"value": rate, "unit": "chain-steps/s", "cores": cores,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": rate, "unit": "chain-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference ships no CPU annealer; this is the oracle's C restatement "
+                    "of its sweep (src/anneal_kernels.cu:262-491), one chain per core",
+        }
+        print(json.dumps(line))
+        return 0
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    res = gpu_arm(args, rank, world)
+    if rank == 0 and not args.no_cpu:
+        rate, cores, sample, _ = cpu_rate(workload_graphs(), 1, 0, args.cpu_seconds)
+        res["cpu_baseline"] = {"value": rate, "unit": "chain-steps/s", "cores": cores,
+                               "kind": "port", "sample": sample}
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(res))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

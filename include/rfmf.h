@@ -1,0 +1,195 @@
+/*
+ * rfmf.h -- C ABI of the GB300-native RFMF annealer (librfmf.so).
+ *
+ * Drop-in boundary for the reference's annealer path (gt-tinker/rfmf).  The
+ * reference's boundary is the C++ function gpu3::annealGpu
+ * (src/anneal_gpu.cuh:76-88, defined at src/anneal_kernels.cu:835-884) plus
+ * the host helpers of src/host_common.h; every entry point below names the
+ * reference interface it replaces.  include/rfmf_annealgpu.hpp re-exposes
+ * gpu3::annealGpu with the reference's exact C++ signature on top of this ABI.
+ *
+ * Conventions: plain pointers and sizes, caller-owned buffers, no CUDA or
+ * torch types.  Every function returns an rfmf_status (never exits or
+ * throws); rfmf_last_error() gives the message of the calling thread's last
+ * failure.  A context owns one device and one CUDA stream; calls on one
+ * context are not thread-safe, separate contexts are independent.
+ *
+ * Spins are int8 +1/-1, one per vertex, chain-major (chain c's vertex v at
+ * c*n + v).  Vertex ids are the dense ids of the reference's AnnealCsr.
+ */
+#ifndef RFMF_H
+#define RFMF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum rfmf_status {
+    RFMF_OK = 0,
+    RFMF_ERR_INVALID = 1,    /* bad argument or malformed graph */
+    RFMF_ERR_CUDA = 2,       /* a CUDA runtime call failed */
+    RFMF_ERR_NOMEM = 3,      /* device or host allocation failed */
+    RFMF_ERR_CAPACITY = 4,   /* request exceeds a documented limit */
+    RFMF_ERR_DEVICE = 5,     /* the kernel reported an inconsistency */
+    RFMF_ERR_BETA_RUNS = 6   /* beta run tables would exceed the run cap */
+} rfmf_status;
+
+typedef struct rfmf_context rfmf_context;
+typedef struct rfmf_graph rfmf_graph;
+typedef struct rfmf_batch rfmf_batch;
+
+/* Library version string. */
+const char* rfmf_version(void);
+
+/* Message of the calling thread's last failing call ("" if none). */
+const char* rfmf_last_error(void);
+
+/* Open a context on CUDA device `device`: replaces the cudaSetDevice and the
+ * default-stream use of src/anneal_kernels.cu:874. */
+int rfmf_context_create(int device, rfmf_context** out);
+int rfmf_context_destroy(rfmf_context* ctx);
+
+/* Device properties the autotuner uses (SM count, opt-in shared memory per
+ * block).  Either pointer may be NULL. */
+int rfmf_context_info(const rfmf_context* ctx, int* sm_count, int* smem_optin);
+
+/*
+ * Upload a CSR graph: n vertices, offsets[n+1], col/weight[offsets[n]].
+ * Replaces the CSR flatten + upload of src/anneal_kernels.cu:666-741 (the
+ * DevCsr of src/anneal_gpu.cuh:23-28) for the AnnealCsr layout of
+ * src/immutable_graph.hpp:36-38.  The CSR must be symmetric (each undirected
+ * edge twice, equal weights), without self loops, rows strictly ascending.
+ * Limits: n < 2^31, offsets[n] < 2^32.
+ */
+int rfmf_graph_create(rfmf_context* ctx, int64_t n, const uint32_t* offsets,
+                      const int32_t* col, const int32_t* weight, rfmf_graph** out);
+int rfmf_graph_destroy(rfmf_graph* g);
+
+/* n, m (undirected edges) and B = max weighted degree; any pointer may be NULL.
+ * B replaces maxWeightedDegree (src/host_common.cpp:314-325). */
+int rfmf_graph_info(const rfmf_graph* g, int64_t* n, int64_t* m,
+                    int64_t* max_weighted_degree);
+
+/* ---- host helpers of src/host_common.{h,cpp}, src/max_cut.cpp, src/rng.hpp */
+
+/* annealTotalSteps (src/host_common.cpp:196-210): sum of iters, capped at
+ * 10^12; returns -1 past the cap. */
+int64_t rfmf_total_steps(int64_t nphases, const uint64_t* iters);
+
+/* betaFixedForStep (src/host_common.h:73-76). */
+int32_t rfmf_beta_fixed(uint64_t step, double t0);
+
+/* annealScoreSafeInt32 (src/host_common.cpp:296-312): 1 if int32 scores are
+ * exact for every sweep of a run of total_steps at temperature t0. */
+int rfmf_score_safe_int32(int64_t total_steps, double t0, int64_t delta_bound);
+
+/* maxWeightedDegree (src/host_common.cpp:314-325) on a host CSR. */
+int64_t rfmf_max_weighted_degree(int64_t n, const uint32_t* offsets,
+                                 const int32_t* weight);
+
+/* cutValueCsr (src/max_cut.cpp:5-15) on a host CSR. */
+int64_t rfmf_cut_value(int64_t n, const uint32_t* offsets, const int32_t* col,
+                       const int32_t* weight, const int8_t* spin);
+
+/* Initial spins of a chain from its RAW seed: xoshiro256++ seeded by
+ * splitmix64, one bit per vertex (src/rng.hpp, src/host_common.cpp:40-45). */
+void rfmf_initial_spins(uint64_t seed, int64_t n, int8_t* out);
+
+/*
+ * buildBetaRunTables (src/host_common.cpp:212-294): run-length beta tables,
+ * one per distinct t0 (exact double equality), runs as (0-based exclusive end
+ * step, beta_fixed).  Writes at most `cap` runs, the run count to *runs and
+ * each chain's first-run index to chain_off[C].  RFMF_ERR_BETA_RUNS past
+ * 33,000,000 runs (kMaxBetaRuns, src/host_common.h:96-99).
+ */
+int rfmf_beta_tables(const double* t0s, int64_t C, int64_t total_steps,
+                     int64_t* run_end, int32_t* run_val, int64_t* chain_off,
+                     int64_t cap, int64_t* runs);
+
+/* ---- the annealer ------------------------------------------------------ */
+
+/* Mirrors gpu3::LaunchConfig (src/anneal_gpu.cuh:52-58) plus the knobs the
+ * reference fixed in src/tuning.hpp.  Zero-initialise for defaults. */
+typedef struct rfmf_launch_config {
+    int corr;              /* CorrMode; accepted, no effect (FLIP needs no corr walk) */
+    int device;            /* informational; the context's device is used */
+    int s_width;           /* 32 or 64; accepted, output-invariant (|D| <= B fits int32) */
+    int threads_per_chain; /* 0 = autotune, else 32, 64, 128 or 256 */
+    int score_path;        /* 0 = gate (src/host_common.cpp:296-312), 1 = int32, 2 = int64 */
+    int reg_variant;       /* 0 = autotune, 1/2/3 = 128/80/64-register kernel */
+    int reserved[2];
+} rfmf_launch_config;
+
+/*
+ * gpu3::annealGpu (src/anneal_gpu.cuh:76-88): run C independent chains over
+ * one graph, chain c with (initial_spins[c], t0s[c], solver_seeds[c]) and the
+ * shared schedule (phases, iters).  Synchronous; host buffers in and out:
+ * end_spins/best_spins C*n int8, kernel_best_vals/kernel_final_vals C int64
+ * (may be NULL), *kernel_ms the device time of the annealing launch(es).
+ * n == 0 or nphases == 0 returns the inputs with cutValueCsr-seeded values
+ * (src/anneal_kernels.cu:856-868).  solver_seeds[c] is the raw seed plus
+ * 0xC2B2AE3D27D4EB4F, as main.cu:27-29 computes it.
+ */
+int rfmf_anneal(rfmf_context* ctx, const rfmf_graph* g, int64_t max_weighted_deg,
+                int64_t C, const int8_t* initial_spins, const double* t0s,
+                int64_t nphases, const uint64_t* phases, const uint64_t* iters,
+                const uint64_t* solver_seeds, const rfmf_launch_config* cfg,
+                int8_t* end_spins, int8_t* best_spins, float* kernel_ms,
+                int64_t* kernel_best_vals, int64_t* kernel_final_vals);
+
+/*
+ * Batched, device-resident form (no reference counterpart: the reference
+ * runs one graph per launch and keeps nothing between calls).  A batch holds
+ * chains over any number of graphs, each with its own t0 and seed, all on one
+ * schedule.  Chain state (spins, best spins, cut values, progress) stays in
+ * device memory between rfmf_batch_run calls; each run advances every
+ * unfinished chain by up to `sweeps` sweeps in ONE persistent launch, and a
+ * sequence of runs equals one uninterrupted anneal bit for bit.
+ *
+ * graphs[c], t0s[c], solver_seeds[c]: per chain.  initial_spins: the chains'
+ * spins concatenated in chain order (n of chain c's graph each).
+ */
+int rfmf_batch_create(rfmf_context* ctx, int64_t nchains, const rfmf_graph* const* graphs,
+                      const double* t0s, const uint64_t* solver_seeds,
+                      const int8_t* initial_spins, int64_t nphases,
+                      const uint64_t* phases, const uint64_t* iters,
+                      const rfmf_launch_config* cfg, rfmf_batch** out);
+
+/* Enqueue one launch advancing every unfinished chain by up to `sweeps`
+ * sweeps, on the context stream; returns without waiting. */
+int rfmf_batch_run(rfmf_batch* b, uint64_t sweeps);
+
+/* Capture `launches` rfmf_batch_run(b, sweeps) steps in a CUDA graph and
+ * replay it `replays` times (fixed-size sweep batches without per-launch
+ * host work).  Asynchronous like rfmf_batch_run. */
+int rfmf_batch_run_graph(rfmf_batch* b, uint64_t sweeps, int launches, int replays);
+
+/* rfmf_batch_run, then wait; *ms receives the device time of the launch
+ * (CUDA events on the context stream). */
+int rfmf_batch_run_timed(rfmf_batch* b, uint64_t sweeps, float* ms);
+
+/* Per chain: number of sweeps so far that raised its best cut (the sweeps on
+ * which the best-spin snapshot was taken).  Synchronous. */
+int rfmf_batch_stats(rfmf_batch* b, uint64_t* improved_sweeps);
+
+/* Wait for the batch's work; reports a device-side error if one occurred. */
+int rfmf_batch_synchronize(rfmf_batch* b);
+
+/* Copy chain state to the host (synchronous).  Any pointer may be NULL.
+ * end_spins/best_spins: concatenated like initial_spins. */
+int rfmf_batch_read(rfmf_batch* b, int8_t* end_spins, int8_t* best_spins,
+                    int64_t* cur_vals, int64_t* best_vals, uint64_t* sweeps_done);
+
+/* Sweeps of the batch's schedule (sum of iters over phases with P != 0). */
+int rfmf_batch_info(const rfmf_batch* b, int64_t* nchains, uint64_t* total_sweeps,
+                    int* threads_per_chain, int* grid, int* score64, int* reg_variant);
+
+int rfmf_batch_destroy(rfmf_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RFMF_H */

@@ -1,0 +1,95 @@
+"""ctypes bindings onto librfmf.so (the C ABI of include/rfmf.h).
+
+The library is the product; this module only loads it and declares the
+signatures.  Loading fails loudly when the library is missing: there is no
+CPU fallback anywhere in the package.
+"""
+import ctypes as ct
+import os
+import pathlib
+
+from . import build as _build
+
+_P = ct.c_void_p
+_I64 = ct.c_int64
+_U64 = ct.c_uint64
+_I32 = ct.c_int32
+
+# (name, restype, argtypes) for every symbol include/rfmf.h declares.
+SIGNATURES = [
+    ("rfmf_version", ct.c_char_p, []),
+    ("rfmf_last_error", ct.c_char_p, []),
+    ("rfmf_context_create", ct.c_int, [ct.c_int, _P]),
+    ("rfmf_context_destroy", ct.c_int, [_P]),
+    ("rfmf_context_info", ct.c_int, [_P, _P, _P]),
+    ("rfmf_graph_create", ct.c_int, [_P, _I64, _P, _P, _P, _P]),
+    ("rfmf_graph_destroy", ct.c_int, [_P]),
+    ("rfmf_graph_info", ct.c_int, [_P, _P, _P, _P]),
+    ("rfmf_total_steps", _I64, [_I64, _P]),
+    ("rfmf_beta_fixed", _I32, [_U64, ct.c_double]),
+    ("rfmf_score_safe_int32", ct.c_int, [_I64, ct.c_double, _I64]),
+    ("rfmf_max_weighted_degree", _I64, [_I64, _P, _P]),
+    ("rfmf_cut_value", _I64, [_I64, _P, _P, _P, _P]),
+    ("rfmf_initial_spins", None, [_U64, _I64, _P]),
+    ("rfmf_beta_tables", ct.c_int, [_P, _I64, _I64, _P, _P, _P, _I64, _P]),
+    ("rfmf_anneal", ct.c_int, [_P, _P, _I64, _I64, _P, _P, _I64, _P, _P, _P, _P,
+                               _P, _P, _P, _P, _P]),
+    ("rfmf_batch_create", ct.c_int, [_P, _I64, _P, _P, _P, _P, _I64, _P, _P, _P, _P]),
+    ("rfmf_batch_run", ct.c_int, [_P, _U64]),
+    ("rfmf_batch_run_graph", ct.c_int, [_P, _U64, ct.c_int, ct.c_int]),
+    ("rfmf_batch_run_timed", ct.c_int, [_P, _U64, _P]),
+    ("rfmf_batch_stats", ct.c_int, [_P, _P]),
+    ("rfmf_batch_synchronize", ct.c_int, [_P]),
+    ("rfmf_batch_read", ct.c_int, [_P, _P, _P, _P, _P, _P]),
+    ("rfmf_batch_info", ct.c_int, [_P, _P, _P, _P, _P, _P, _P]),
+    ("rfmf_batch_destroy", ct.c_int, [_P]),
+]
+
+
+class LaunchConfig(ct.Structure):
+    """rfmf_launch_config (mirrors gpu3::LaunchConfig plus tuning knobs)."""
+    _fields_ = [("corr", ct.c_int), ("device", ct.c_int), ("s_width", ct.c_int),
+                ("threads_per_chain", ct.c_int), ("score_path", ct.c_int),
+                ("reg_variant", ct.c_int), ("reserved", ct.c_int * 2)]
+
+
+STATUS = {0: "RFMF_OK", 1: "RFMF_ERR_INVALID", 2: "RFMF_ERR_CUDA", 3: "RFMF_ERR_NOMEM",
+          4: "RFMF_ERR_CAPACITY", 5: "RFMF_ERR_DEVICE", 6: "RFMF_ERR_BETA_RUNS"}
+
+
+class RfmfError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def library_path():
+    return pathlib.Path(os.environ.get("RFMF_LIB", str(_build.LIB)))
+
+
+def lib(build_if_missing=True):
+    """Load librfmf.so (building it first if absent and nvcc is available)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not path.exists() and build_if_missing:
+        _build.build()
+    if not path.exists():
+        raise RuntimeError(f"librfmf.so not found at {path}; run rfmf_gb300.build.build()")
+    L = ct.CDLL(str(path))
+    for name, res, args in SIGNATURES:
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(code):
+    if code != 0:
+        raise RfmfError(code, lib().rfmf_last_error().decode(errors="replace"))
+    return code

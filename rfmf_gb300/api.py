@@ -1,0 +1,253 @@
+"""Python mirror of the reference's annealer interface over the C ABI.
+
+Names and argument meanings follow the reference (gt-tinker/rfmf):
+anneal_gpu <-> gpu3::annealGpu (src/anneal_gpu.cuh:76-88), LaunchConfig <->
+gpu3::LaunchConfig (src/anneal_gpu.cuh:52-58), the helpers <->
+src/host_common.h.  Every call goes through librfmf.so; errors raise
+RfmfError instead of exiting.
+"""
+import ctypes as ct
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._lib import LaunchConfig, RfmfError, check, lib
+
+# Offset between a chain's raw seed (initial spins) and its Philox solver seed
+# (src/host_common.h:22-25, main.cu:27-29).
+SOLVER_SEED_OFFSET = 0xC2B2AE3D27D4EB4F
+
+
+def solver_seed(seed):
+    return (int(seed) + SOLVER_SEED_OFFSET) % 2**64
+
+
+def _p(a):
+    return a.ctypes.data if a is not None else None
+
+
+def version():
+    return lib().rfmf_version().decode()
+
+
+def initial_spins(seed, n):
+    """Chain's initial spins from its RAW seed (src/host_common.cpp:40-45)."""
+    out = np.zeros(n, np.int8)
+    lib().rfmf_initial_spins(int(seed) % 2**64, n, _p(out))
+    return out
+
+
+def total_steps(iters):
+    it = np.ascontiguousarray(iters, np.uint64)
+    r = lib().rfmf_total_steps(len(it), _p(it))
+    if r < 0:
+        raise RfmfError(4, "iters total more than 10^12 sweeps")
+    return r
+
+
+def beta_fixed(step, t0):
+    return lib().rfmf_beta_fixed(int(step), float(t0))
+
+
+def score_safe_int32(total, t0, B):
+    return bool(lib().rfmf_score_safe_int32(int(total), float(t0), int(B)))
+
+
+def max_weighted_degree(g):
+    return lib().rfmf_max_weighted_degree(g.n, _p(g.offsets), _p(g.weight))
+
+
+def cut_value(g, spin):
+    spin = np.ascontiguousarray(spin, np.int8)
+    return lib().rfmf_cut_value(g.n, _p(g.offsets), _p(g.col), _p(g.weight), _p(spin))
+
+
+def beta_tables(t0s, total):
+    """buildBetaRunTables: returns (run_end int64, run_val int32, chain_off)."""
+    t = np.ascontiguousarray(t0s, np.float64)
+    runs = ct.c_int64(0)
+    off = np.zeros(len(t), np.int64)
+    check(lib().rfmf_beta_tables(_p(t), len(t), int(total), None, None, _p(off), 0,
+                                 ct.byref(runs)))
+    end = np.zeros(runs.value, np.int64)
+    val = np.zeros(runs.value, np.int32)
+    check(lib().rfmf_beta_tables(_p(t), len(t), int(total), _p(end), _p(val), _p(off),
+                                 runs.value, ct.byref(runs)))
+    return end, val, off
+
+
+def make_config(threads_per_chain=0, score_path=0, reg_variant=0, corr=0, s_width=32,
+                device=0):
+    c = LaunchConfig()
+    c.corr = corr
+    c.device = device
+    c.s_width = s_width
+    c.threads_per_chain = threads_per_chain
+    c.score_path = score_path
+    c.reg_variant = reg_variant
+    return c
+
+
+class Context:
+    """One CUDA device + stream (rfmf_context)."""
+
+    def __init__(self, device=0):
+        h = ct.c_void_p()
+        check(lib().rfmf_context_create(device, ct.byref(h)))
+        self.h = h
+        self.device = device
+
+    def info(self):
+        sms, smem = ct.c_int(0), ct.c_int(0)
+        check(lib().rfmf_context_info(self.h, ct.byref(sms), ct.byref(smem)))
+        return dict(sm_count=sms.value, smem_optin=smem.value)
+
+    def close(self):
+        if self.h:
+            lib().rfmf_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceGraph:
+    """A CSR graph resident in device memory (rfmf_graph)."""
+
+    def __init__(self, ctx, g):
+        h = ct.c_void_p()
+        self.off = np.ascontiguousarray(g.offsets, np.uint32)
+        self.col = np.ascontiguousarray(g.col, np.int32)
+        self.w = np.ascontiguousarray(g.weight, np.int32)
+        check(lib().rfmf_graph_create(ctx.h, g.n, _p(self.off), _p(self.col), _p(self.w),
+                                      ct.byref(h)))
+        self.h = h
+        self.ctx = ctx
+        self.g = g
+        self.n = g.n
+
+    def info(self):
+        n, m, B = ct.c_int64(), ct.c_int64(), ct.c_int64()
+        check(lib().rfmf_graph_info(self.h, ct.byref(n), ct.byref(m), ct.byref(B)))
+        return dict(n=n.value, m=m.value, max_weighted_degree=B.value)
+
+    def close(self):
+        if self.h:
+            lib().rfmf_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class AnnealResult:
+    end_spins: np.ndarray
+    best_spins: np.ndarray
+    kernel_ms: float
+    best_vals: np.ndarray
+    final_vals: np.ndarray
+
+
+def anneal_gpu(ctx, dgraph, max_weighted_deg, initial_spins_, t0s, phases, iters, solver_seeds,
+               cfg=None):
+    """gpu3::annealGpu: C chains over one graph, host buffers in and out."""
+    spins = np.ascontiguousarray(initial_spins_, np.int8)
+    C = spins.shape[0]
+    n = dgraph.n
+    assert spins.shape == (C, n)
+    t = np.ascontiguousarray(t0s, np.float64)
+    ph = np.ascontiguousarray(phases, np.uint64)
+    it = np.ascontiguousarray(iters, np.uint64)
+    sd = np.array([int(s) % 2**64 for s in solver_seeds], np.uint64)
+    assert len(t) == C and len(sd) == C and len(ph) == len(it)
+    end = np.zeros((C, n), np.int8)
+    best = np.zeros((C, n), np.int8)
+    bv = np.zeros(C, np.int64)
+    fv = np.zeros(C, np.int64)
+    ms = ct.c_float(0)
+    cfg = cfg or make_config()
+    check(lib().rfmf_anneal(ctx.h, dgraph.h, int(max_weighted_deg), C, _p(spins), _p(t),
+                            len(ph), _p(ph), _p(it), _p(sd), ct.byref(cfg), _p(end), _p(best),
+                            ct.byref(ms), _p(bv), _p(fv)))
+    return AnnealResult(end, best, ms.value, bv, fv)
+
+
+class Batch:
+    """Chains over many graphs with device-resident state (rfmf_batch)."""
+
+    def __init__(self, ctx, dgraphs, t0s, solver_seeds, init_spins, phases, iters, cfg=None):
+        C = len(dgraphs)
+        self.C = C
+        self.ns = [g.n for g in dgraphs]
+        self.ctx = ctx
+        self.dgraphs = list(dgraphs)   # keep alive
+        garr = (ct.c_void_p * C)(*[g.h.value for g in dgraphs])
+        t = np.ascontiguousarray(t0s, np.float64)
+        sd = np.array([int(s) % 2**64 for s in solver_seeds], np.uint64)
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(s, np.int8) for s in init_spins]))
+        assert len(flat) == sum(self.ns)
+        ph = np.ascontiguousarray(phases, np.uint64)
+        it = np.ascontiguousarray(iters, np.uint64)
+        cfg = cfg or make_config()
+        h = ct.c_void_p()
+        check(lib().rfmf_batch_create(ctx.h, C, garr, _p(t), _p(sd), _p(flat), len(ph),
+                                      _p(ph), _p(it), ct.byref(cfg), ct.byref(h)))
+        self.h = h
+
+    def info(self):
+        C, tot = ct.c_int64(), ct.c_uint64()
+        th, gr, s64, var = ct.c_int(), ct.c_int(), ct.c_int(), ct.c_int()
+        check(lib().rfmf_batch_info(self.h, ct.byref(C), ct.byref(tot), ct.byref(th),
+                                    ct.byref(gr), ct.byref(s64), ct.byref(var)))
+        return dict(nchains=C.value, total_sweeps=tot.value, threads_per_chain=th.value,
+                    grid=gr.value, score64=bool(s64.value), reg_variant=var.value)
+
+    def run(self, sweeps):
+        check(lib().rfmf_batch_run(self.h, int(sweeps)))
+
+    def run_graph(self, sweeps, launches=1, replays=1):
+        check(lib().rfmf_batch_run_graph(self.h, int(sweeps), int(launches), int(replays)))
+
+    def run_timed(self, sweeps):
+        """Launch, wait, and return the launch's device time in ms."""
+        ms = ct.c_float(0)
+        check(lib().rfmf_batch_run_timed(self.h, int(sweeps), ct.byref(ms)))
+        return ms.value
+
+    def improved_sweeps(self):
+        out = np.zeros(self.C, np.uint64)
+        check(lib().rfmf_batch_stats(self.h, _p(out)))
+        return out
+
+    def synchronize(self):
+        check(lib().rfmf_batch_synchronize(self.h))
+
+    def read(self):
+        tot = sum(self.ns)
+        end = np.zeros(tot, np.int8)
+        best = np.zeros(tot, np.int8)
+        cur = np.zeros(self.C, np.int64)
+        bv = np.zeros(self.C, np.int64)
+        done = np.zeros(self.C, np.uint64)
+        check(lib().rfmf_batch_read(self.h, _p(end), _p(best), _p(cur), _p(bv), _p(done)))
+        splits = np.cumsum(self.ns)[:-1]
+        return dict(end_spins=np.split(end, splits), best_spins=np.split(best, splits),
+                    cur_vals=cur, best_vals=bv, sweeps_done=done)
+
+    def close(self):
+        if self.h:
+            lib().rfmf_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

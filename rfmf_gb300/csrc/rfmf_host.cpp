@@ -1,0 +1,877 @@
+// rfmf_host.cpp -- host side of librfmf.so: the C ABI of include/rfmf.h.
+//
+// Replaces the reference's host driver (src/anneal_kernels.cu:498-884:
+// runDispatch/runMC/annealGpu) and the helpers of src/host_common.cpp it
+// calls.  Differences by design: errors are status codes (the reference
+// exits), device state can stay resident across calls (batches), many graphs
+// share one persistent launch, and the launch geometry comes from an
+// occupancy-driven autotuner instead of the V100 constants of src/tuning.hpp.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/rfmf.h"
+#include "rfmf_device.h"
+
+namespace rfmf {
+size_t smem_bytes(int maxN, int maxWords, int pmax);
+const void* kernel_ptr(bool score64, int variant);
+int num_variants();
+cudaError_t launch_anneal(const DevLaunch& L, bool score64, int variant, int grid, int threads,
+                          size_t smem, int pmax, cudaStream_t stream);
+}  // namespace rfmf
+
+using namespace rfmf;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CU(call)                                                                 \
+    do {                                                                         \
+        const cudaError_t e_ = (call);                                           \
+        if (e_ != cudaSuccess)                                                   \
+            return fail(e_ == cudaErrorMemoryAllocation ? RFMF_ERR_NOMEM         \
+                                                        : RFMF_ERR_CUDA,         \
+                        "%s failed: %s", #call, cudaGetErrorString(e_));         \
+    } while (0)
+
+constexpr uint64_t kMaxTotalSteps = 1000000000000ull;   // src/host_common.h:80
+constexpr int64_t kMaxBetaRuns = 33000000;              // src/host_common.h:99
+constexpr int64_t kGumbelMaxMag = 3617486 + 127;        // src/philox.cuh:44-48
+
+// Q20 Gumbel quantile table: round(-log(-log((2i+1)/32)) * 2^20), the
+// defining formula of src/philox.cuh:26-34 (every entry >= 0.016 away from a
+// rounding boundary, so the double evaluation is exact).
+void gumbel_lut(int32_t lut[16]) {
+    for (int i = 0; i < 16; ++i)
+        lut[i] = static_cast<int32_t>(std::lround(-std::log(-std::log((2.0 * i + 1.0) / 32.0)) *
+                                                  1048576.0));
+}
+
+// betaFixedForStep: round(log(1+step)/t0 * 2^20) in host double
+// (src/host_common.h:73-76).  Never evaluated on the device.
+inline int32_t beta_fixed(uint64_t step, double t0) {
+    const double beta = std::log(1.0 + static_cast<double>(step)) / t0;
+    return static_cast<int32_t>(std::round(beta * (1 << 20)));
+}
+
+// First 1-based step > s0 whose beta exceeds v.  Starts from the inverse of
+// the schedule (beta crosses v+1/2 at step ~ exp((v+1/2) t0 / 2^20) - 1) and
+// settles the exact boundary with the same double expression the kernel's
+// schedule is defined by, so the table reproduces beta_fixed step for step.
+// Returns 0 if beta stays <= v through `total`.
+int64_t next_run_start(double t0, int32_t v, int64_t s0, int64_t total) {
+    if (beta_fixed(static_cast<uint64_t>(total), t0) <= v) return 0;
+    const double guess = std::exp((static_cast<double>(v) + 0.5) * t0 / 1048576.0) - 1.0;
+    int64_t s = (guess >= static_cast<double>(total)) ? total
+              : std::max<int64_t>(s0 + 1, static_cast<int64_t>(std::ceil(guess)));
+    s = std::min(s, total);
+    // Bracket [lo, hi]: beta(lo) <= v < beta(hi), growing the step outward.
+    int64_t lo = s0, hi = s;
+    if (beta_fixed(static_cast<uint64_t>(hi), t0) <= v) {
+        int64_t span = 1;
+        lo = hi;
+        while (true) {
+            hi = std::min(total, lo + span);
+            if (beta_fixed(static_cast<uint64_t>(hi), t0) > v) break;
+            lo = hi;
+            span *= 2;
+        }
+    } else {
+        int64_t span = 1;
+        while (true) {
+            const int64_t cand = std::max(s0, hi - span);
+            if (cand == s0 || beta_fixed(static_cast<uint64_t>(cand), t0) <= v) {
+                lo = cand;
+                break;
+            }
+            hi = cand;
+            span *= 2;
+        }
+    }
+    while (hi - lo > 1) {
+        const int64_t mid = lo + (hi - lo) / 2;
+        if (beta_fixed(static_cast<uint64_t>(mid), t0) <= v) lo = mid; else hi = mid;
+    }
+    return hi;
+}
+
+// One t0's run-length table over 1-based steps [1, total]; ends are 0-based
+// exclusive (src/host_common.h:82-94).  >= 1 run even when total == 0.
+int append_runs(double t0, int64_t total, std::vector<int64_t>& end, std::vector<int32_t>& val) {
+    if (total <= 0) {
+        end.push_back(0);
+        val.push_back(0);
+        return RFMF_OK;
+    }
+    int64_t s = 1;
+    while (true) {
+        if (static_cast<int64_t>(end.size()) >= kMaxBetaRuns)
+            return fail(RFMF_ERR_BETA_RUNS,
+                        "beta run tables exceed %lld runs (t0=%g, %lld sweeps); runs scale "
+                        "with log(sweeps)/t0 * 2^20",
+                        static_cast<long long>(kMaxBetaRuns), t0, static_cast<long long>(total));
+        const int32_t v = beta_fixed(static_cast<uint64_t>(s), t0);
+        const int64_t nxt = next_run_start(t0, v, s, total);
+        if (nxt == 0) {
+            end.push_back(total);
+            val.push_back(v);
+            return RFMF_OK;
+        }
+        end.push_back(nxt - 1);
+        val.push_back(v);
+        s = nxt;
+    }
+}
+
+struct BetaTables {
+    std::vector<int64_t> end;
+    std::vector<int32_t> val;
+    std::vector<int64_t> chainOff;
+    std::vector<int64_t> chainRuns;
+};
+
+int build_beta(const double* t0s, int64_t C, int64_t total, BetaTables& bt) {
+    std::vector<double> distinct;
+    std::vector<int64_t> first, count;
+    bt.chainOff.resize(C);
+    bt.chainRuns.resize(C);
+    for (int64_t c = 0; c < C; ++c) {
+        size_t k = 0;
+        while (k < distinct.size() && distinct[k] != t0s[c]) ++k;
+        if (k == distinct.size()) {
+            distinct.push_back(t0s[c]);
+            first.push_back(static_cast<int64_t>(bt.end.size()));
+            const int rc = append_runs(t0s[c], total, bt.end, bt.val);
+            if (rc != RFMF_OK) return rc;
+            count.push_back(static_cast<int64_t>(bt.end.size()) - first.back());
+        }
+        bt.chainOff[c] = first[k];
+        bt.chainRuns[c] = count[k];
+    }
+    return RFMF_OK;
+}
+
+bool score_safe_int32(int64_t total, double t0, int64_t B) {
+    // src/host_common.cpp:296-312
+    const double bmax = std::log(1.0 + static_cast<double>(total)) / t0;
+    const int64_t bmf = static_cast<int64_t>(std::llround(bmax * (1 << 20)));
+    const int64_t limit = static_cast<int64_t>(std::numeric_limits<int32_t>::max()) - kGumbelMaxMag;
+    if (bmf > 0 && B > 0 && B > limit / bmf) return false;
+    return (bmf * B + kGumbelMaxMag) < static_cast<int64_t>(std::numeric_limits<int32_t>::max());
+}
+
+// Owning device buffer.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() { if (p) cudaFree(p); }
+    int alloc(size_t b) {
+        bytes = std::max<size_t>(b, 16);
+        const cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return fail(e == cudaErrorMemoryAllocation ? RFMF_ERR_NOMEM : RFMF_ERR_CUDA,
+                        "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+        }
+        return RFMF_OK;
+    }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace
+
+struct rfmf_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int sms = 0;
+    int smemOptin = 0;
+    int32_t lut[16];
+};
+
+struct rfmf_graph {
+    rfmf_context* ctx = nullptr;
+    int64_t n = 0, m = 0, B = 0, wsum2 = 0;
+    DevBuf offsets, edges;
+};
+
+struct rfmf_batch {
+    rfmf_context* ctx = nullptr;
+    int64_t C = 0;
+    uint64_t total = 0;
+    bool score64 = false;
+    int threads = 0, grid = 0, pmax = 0, variant = 0;
+    size_t smem = 0;
+    std::vector<int64_t> chainN, chainWordOff;   // per chain
+    std::vector<int64_t> graphOfChain;
+    int64_t words = 0;                           // total spin words over chains
+    DevBuf dGraphs, dScheds, dChains, dOrder, dPhaseP, dPhaseIters, dBetaEnd, dBetaVal,
+        dBits, dBest, dCtl;
+    DevLaunch L{};
+    cudaGraphExec_t graphExec = nullptr;
+    uint64_t graphSweeps = 0;
+    int graphLaunches = 0;
+    ~rfmf_batch() { if (graphExec) cudaGraphExecDestroy(graphExec); }
+};
+
+// ------------------------------------------------------------------ misc
+extern "C" const char* rfmf_version(void) { return "rfmf_gb300 0.1 (sm_103a)"; }
+extern "C" const char* rfmf_last_error(void) { return g_err.c_str(); }
+
+extern "C" int rfmf_context_create(int device, rfmf_context** out) {
+    if (!out) return fail(RFMF_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    int count = 0;
+    CU(cudaGetDeviceCount(&count));
+    if (device < 0 || device >= count)
+        return fail(RFMF_ERR_INVALID, "device %d out of range (%d devices)", device, count);
+    CU(cudaSetDevice(device));
+    auto ctx = std::unique_ptr<rfmf_context>(new (std::nothrow) rfmf_context());
+    if (!ctx) return fail(RFMF_ERR_NOMEM, "host allocation failed");
+    ctx->device = device;
+    CU(cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device));
+    CU(cudaDeviceGetAttribute(&ctx->smemOptin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    CU(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    gumbel_lut(ctx->lut);
+    *out = ctx.release();
+    return RFMF_OK;
+}
+
+extern "C" int rfmf_context_destroy(rfmf_context* ctx) {
+    if (!ctx) return RFMF_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return RFMF_OK;
+}
+
+extern "C" int rfmf_context_info(const rfmf_context* ctx, int* sm_count, int* smem_optin) {
+    if (!ctx) return fail(RFMF_ERR_INVALID, "ctx is NULL");
+    if (sm_count) *sm_count = ctx->sms;
+    if (smem_optin) *smem_optin = ctx->smemOptin;
+    return RFMF_OK;
+}
+
+// ----------------------------------------------------------- host helpers
+extern "C" int64_t rfmf_total_steps(int64_t nphases, const uint64_t* iters) {
+    // src/host_common.cpp:196-210: summed and range-checked in unsigned.
+    uint64_t total = 0;
+    for (int64_t i = 0; i < nphases; ++i) {
+        total += iters[i];
+        if (iters[i] > kMaxTotalSteps || total > kMaxTotalSteps) return -1;
+    }
+    return static_cast<int64_t>(total);
+}
+
+extern "C" int32_t rfmf_beta_fixed(uint64_t step, double t0) { return beta_fixed(step, t0); }
+
+extern "C" int rfmf_score_safe_int32(int64_t total_steps, double t0, int64_t delta_bound) {
+    return score_safe_int32(total_steps, t0, delta_bound) ? 1 : 0;
+}
+
+extern "C" int64_t rfmf_max_weighted_degree(int64_t n, const uint32_t* offsets,
+                                            const int32_t* weight) {
+    int64_t B = 0;
+    for (int64_t v = 0; v < n; ++v) {
+        int64_t s = 0;
+        for (uint32_t i = offsets[v]; i < offsets[v + 1]; ++i)
+            s += std::llabs(static_cast<long long>(weight[i]));
+        B = std::max(B, s);
+    }
+    return B;
+}
+
+extern "C" int64_t rfmf_cut_value(int64_t n, const uint32_t* offsets, const int32_t* col,
+                                  const int32_t* weight, const int8_t* spin) {
+    int64_t value = 0;
+    for (int64_t v = 0; v < n; ++v)
+        for (uint32_t i = offsets[v]; i < offsets[v + 1]; ++i)
+            if (static_cast<int64_t>(col[i]) > v && spin[v] != spin[col[i]]) value += weight[i];
+    return value;
+}
+
+extern "C" void rfmf_initial_spins(uint64_t seed, int64_t n, int8_t* out) {
+    // xoshiro256++ (Blackman & Vigna) seeded by splitmix64; bits drawn one at
+    // a time from a 64-bit reservoir, 1 -> +1 (src/rng.hpp:11-58).
+    uint64_t s[4];
+    uint64_t z = seed;
+    for (auto& w : s) {
+        z += 0x9e3779b97f4a7c15ULL;
+        uint64_t x = z;
+        x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ULL;
+        x = (x ^ (x >> 27)) * 0x94d049bb133111ebULL;
+        w = x ^ (x >> 31);
+    }
+    auto rotl = [](uint64_t x, int k) { return (x << k) | (x >> (64 - k)); };
+    uint64_t buf = 0;
+    int avail = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        if (avail == 0) {
+            buf = rotl(s[0] + s[3], 23) + s[0];
+            const uint64_t t = s[1] << 17;
+            s[2] ^= s[0];
+            s[3] ^= s[1];
+            s[1] ^= s[2];
+            s[0] ^= s[3];
+            s[2] ^= t;
+            s[3] = rotl(s[3], 45);
+            avail = 64;
+        }
+        out[i] = (buf & 1u) ? 1 : -1;
+        buf >>= 1;
+        --avail;
+    }
+}
+
+extern "C" int rfmf_beta_tables(const double* t0s, int64_t C, int64_t total_steps,
+                                int64_t* run_end, int32_t* run_val, int64_t* chain_off,
+                                int64_t cap, int64_t* runs) {
+    if (C < 0 || (C > 0 && !t0s) || total_steps < 0) return fail(RFMF_ERR_INVALID, "bad arguments");
+    for (int64_t c = 0; c < C; ++c)
+        if (!(t0s[c] > 0.0)) return fail(RFMF_ERR_INVALID, "t0s[%lld] must be > 0", (long long)c);
+    BetaTables bt;
+    const int rc = build_beta(t0s, C, total_steps, bt);
+    if (rc != RFMF_OK) return rc;
+    const int64_t R = static_cast<int64_t>(bt.end.size());
+    for (int64_t i = 0; i < R && i < cap; ++i) {
+        if (run_end) run_end[i] = bt.end[i];
+        if (run_val) run_val[i] = bt.val[i];
+    }
+    if (chain_off) for (int64_t c = 0; c < C; ++c) chain_off[c] = bt.chainOff[c];
+    if (runs) *runs = R;
+    return RFMF_OK;
+}
+
+// ------------------------------------------------------------------ graph
+extern "C" int rfmf_graph_create(rfmf_context* ctx, int64_t n, const uint32_t* offsets,
+                                 const int32_t* col, const int32_t* weight, rfmf_graph** out) {
+    if (!ctx || !out) return fail(RFMF_ERR_INVALID, "ctx/out is NULL");
+    *out = nullptr;
+    if (n < 0 || n >= (int64_t(1) << 31)) return fail(RFMF_ERR_INVALID, "n=%lld out of range", (long long)n);
+    if (!offsets) return fail(RFMF_ERR_INVALID, "offsets is NULL");
+    if (offsets[0] != 0) return fail(RFMF_ERR_INVALID, "offsets[0] must be 0");
+    const uint64_t m2 = offsets[n];
+    if (m2 > 0 && (!col || !weight)) return fail(RFMF_ERR_INVALID, "col/weight is NULL");
+    // Validate: monotone offsets, ids in range, rows strictly ascending, no
+    // self loops, symmetric with equal weights (the AnnealCsr invariants the
+    // kernel's per-vertex gain bookkeeping relies on).
+    int64_t B = 0, wsum2 = 0;
+    for (int64_t v = 0; v < n; ++v) {
+        if (offsets[v + 1] < offsets[v]) return fail(RFMF_ERR_INVALID, "offsets not monotone at %lld", (long long)v);
+        int64_t s = 0;
+        for (uint32_t i = offsets[v]; i < offsets[v + 1]; ++i) {
+            const int32_t u = col[i];
+            if (u < 0 || u >= n) return fail(RFMF_ERR_INVALID, "col[%u]=%d out of range", i, u);
+            if (u == v) return fail(RFMF_ERR_INVALID, "self loop at vertex %lld", (long long)v);
+            if (i > offsets[v] && col[i - 1] >= u)
+                return fail(RFMF_ERR_INVALID, "row %lld not strictly ascending", (long long)v);
+            // symmetric entry (u, v) with the same weight
+            const int32_t* b = col + offsets[u];
+            const int32_t* e = col + offsets[u + 1];
+            const int32_t* f = std::lower_bound(b, e, static_cast<int32_t>(v));
+            if (f == e || *f != v || weight[f - col] != weight[i])
+                return fail(RFMF_ERR_INVALID, "edge (%lld,%d) has no symmetric twin", (long long)v, u);
+            s += std::llabs(static_cast<long long>(weight[i]));
+            wsum2 += weight[i];
+        }
+        B = std::max(B, s);
+    }
+    if (B > std::numeric_limits<int32_t>::max())
+        return fail(RFMF_ERR_CAPACITY, "max weighted degree %lld exceeds int32", (long long)B);
+    CU(cudaSetDevice(ctx->device));
+    auto g = std::unique_ptr<rfmf_graph>(new (std::nothrow) rfmf_graph());
+    if (!g) return fail(RFMF_ERR_NOMEM, "host allocation failed");
+    g->ctx = ctx;
+    g->n = n;
+    g->m = static_cast<int64_t>(m2 / 2);
+    g->B = B;
+    g->wsum2 = wsum2;
+    std::vector<Edge> he(m2);
+    for (uint64_t i = 0; i < m2; ++i) he[i] = Edge{col[i], weight[i]};
+    int rc = g->offsets.alloc((n + 1) * sizeof(uint32_t));
+    if (rc) return rc;
+    rc = g->edges.alloc(m2 * sizeof(Edge));
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(g->offsets.p, offsets, (n + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream));
+    if (m2) CU(cudaMemcpyAsync(g->edges.p, he.data(), m2 * sizeof(Edge), cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    *out = g.release();
+    return RFMF_OK;
+}
+
+extern "C" int rfmf_graph_destroy(rfmf_graph* g) {
+    if (!g) return RFMF_OK;
+    cudaSetDevice(g->ctx->device);
+    delete g;
+    return RFMF_OK;
+}
+
+extern "C" int rfmf_graph_info(const rfmf_graph* g, int64_t* n, int64_t* m, int64_t* B) {
+    if (!g) return fail(RFMF_ERR_INVALID, "graph is NULL");
+    if (n) *n = g->n;
+    if (m) *m = g->m;
+    if (B) *B = g->B;
+    return RFMF_OK;
+}
+
+// ------------------------------------------------------------------ batch
+namespace {
+
+// Launch geometry.  Candidates: threads per chain-CTA T in {256..32} (capped
+// so each thread owns at least two Philox blocks of the largest graph) times
+// the register-budget variants (128/80/64 registers).  Preference: every chain
+// resident at once (no tail wave), then the most threads per chain, then the
+// largest register budget.  Grid: every resident CTA slot, up to one per
+// chain (persistent work queue).
+int autotune(rfmf_batch& b, int requestedT, int requestedVariant, int maxN) {
+    const int nv = num_variants();
+    // Every variant may use the device's full opt-in shared memory, so a
+    // launch of any batch stays legal whichever batch set the attribute
+    // last; occupancy below is computed for this batch's actual size.  The
+    // carveout prefers shared memory (chain state) over L1.
+    for (int v = 0; v < nv; ++v) {
+        const void* kern = kernel_ptr(b.score64, v);
+        cudaFuncAttributes fa{};
+        CU(cudaFuncGetAttributes(&fa, kern));
+        const int dynMax = b.ctx->smemOptin - static_cast<int>(fa.sharedSizeBytes);
+        if (static_cast<int>(b.smem) > dynMax)
+            return fail(RFMF_ERR_CAPACITY,
+                        "chain state needs %zu B of shared memory but %d B are available "
+                        "per CTA", b.smem, dynMax);
+        CU(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dynMax));
+        CU(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                cudaSharedmemCarveoutMaxShared));
+    }
+    auto occ_for = [&](int t, int v) -> int {
+        const void* kern = kernel_ptr(b.score64, v);
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, t, b.smem) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        return occ;
+    };
+    const int nblk = (maxN + 7) / 8;
+    int tcap = 32;
+    while (tcap * 2 <= 256 && tcap * 2 * 2 <= nblk) tcap *= 2;
+    int bestT = 0, bestV = 0, bestOcc = 0;
+    bool bestAll = false;
+    for (int t = 256; t >= 32; t /= 2) {
+        if (requestedT ? (t != requestedT) : (t > tcap)) continue;
+        for (int v = 0; v < nv; ++v) {
+            if (requestedVariant >= 0 && v != requestedVariant) continue;
+            const int occ = occ_for(t, v);
+            if (occ <= 0) continue;
+            const bool all = static_cast<int64_t>(occ) * b.ctx->sms >= b.C;
+            if (!bestT || (all && !bestAll)) {
+                bestT = t; bestV = v; bestOcc = occ; bestAll = all;
+            }
+        }
+    }
+    if (!bestT)
+        return fail(RFMF_ERR_CAPACITY,
+                    "no resident CTA configuration with %zu B of shared memory "
+                    "(graph too large for shared-memory residency)", b.smem);
+    b.threads = bestT;
+    b.variant = bestV;
+    b.grid = static_cast<int>(std::min<int64_t>(b.C, static_cast<int64_t>(bestOcc) * b.ctx->sms));
+    return RFMF_OK;
+}
+
+}  // namespace
+
+extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph* const* graphs,
+                                 const double* t0s, const uint64_t* solver_seeds,
+                                 const int8_t* initial_spins, int64_t nphases,
+                                 const uint64_t* phases, const uint64_t* iters,
+                                 const rfmf_launch_config* cfg, rfmf_batch** out) {
+    if (!ctx || !out) return fail(RFMF_ERR_INVALID, "ctx/out is NULL");
+    *out = nullptr;
+    if (C <= 0 || C > (int64_t(1) << 30)) return fail(RFMF_ERR_INVALID, "nchains=%lld", (long long)C);
+    if (!graphs || !t0s || !solver_seeds || !initial_spins)
+        return fail(RFMF_ERR_INVALID, "NULL per-chain array");
+    if (nphases < 0 || (nphases > 0 && (!phases || !iters)))
+        return fail(RFMF_ERR_INVALID, "bad phases/iters");
+    rfmf_launch_config dflt{};
+    const rfmf_launch_config& c = cfg ? *cfg : dflt;
+    if (c.threads_per_chain && (c.threads_per_chain != 32 && c.threads_per_chain != 64 &&
+                                c.threads_per_chain != 128 && c.threads_per_chain != 256))
+        return fail(RFMF_ERR_INVALID, "threads_per_chain must be 0, 32, 64, 128 or 256");
+    if (c.reg_variant < 0 || c.reg_variant > num_variants())
+        return fail(RFMF_ERR_INVALID, "register variant must be 0 (auto) or 1..%d", num_variants());
+    const int64_t totalAll = rfmf_total_steps(nphases, iters);   // src/host_common.cpp:196
+    if (totalAll < 0) return fail(RFMF_ERR_CAPACITY, "iters total more than 10^12 sweeps");
+    uint64_t total = 0, maxP = 0;
+    for (int64_t p = 0; p < nphases; ++p) {
+        if (phases[p] > 0x7FFFFFFFull) return fail(RFMF_ERR_CAPACITY, "phase P too large");
+        if (phases[p]) { total += iters[p]; maxP = std::max<uint64_t>(maxP, phases[p]); }
+    }
+    for (int64_t i = 0; i < C; ++i) {
+        if (!graphs[i] || graphs[i]->ctx != ctx) return fail(RFMF_ERR_INVALID, "graph %lld invalid", (long long)i);
+        if (graphs[i]->n == 0) return fail(RFMF_ERR_INVALID, "chain %lld: graph has no vertices", (long long)i);
+        if (!(t0s[i] > 0.0)) return fail(RFMF_ERR_INVALID, "t0s[%lld] must be > 0", (long long)i);
+    }
+    CU(cudaSetDevice(ctx->device));
+
+    auto b = std::unique_ptr<rfmf_batch>(new (std::nothrow) rfmf_batch());
+    if (!b) return fail(RFMF_ERR_NOMEM, "host allocation failed");
+    b->ctx = ctx;
+    b->C = C;
+    b->total = total;
+
+    // Graph table (distinct graphs in first-use order).
+    std::map<const rfmf_graph*, int> gidx;
+    std::vector<const rfmf_graph*> glist;
+    b->graphOfChain.resize(C);
+    for (int64_t i = 0; i < C; ++i) {
+        auto it = gidx.find(graphs[i]);
+        if (it == gidx.end()) {
+            it = gidx.emplace(graphs[i], static_cast<int>(glist.size())).first;
+            glist.push_back(graphs[i]);
+        }
+        b->graphOfChain[i] = it->second;
+    }
+    int maxN = 0, maxWords = 0;
+    std::vector<DevGraph> hg(glist.size());
+    for (size_t k = 0; k < glist.size(); ++k) {
+        const rfmf_graph* g = glist[k];
+        hg[k].offsets = g->offsets.as<uint32_t>();
+        hg[k].edges = g->edges.as<Edge>();
+        hg[k].n = static_cast<int32_t>(g->n);
+        hg[k].words = static_cast<int32_t>((g->n + 31) / 32);
+        hg[k].wsum2 = g->wsum2;
+        maxN = std::max<int>(maxN, hg[k].n);
+        maxWords = std::max<int>(maxWords, hg[k].words);
+    }
+
+    // Score path: the reference's gate (src/host_common.cpp:296-312) at each
+    // chain's (t0, B); one verdict for the launch.
+    b->score64 = false;
+    if (c.score_path == 2) b->score64 = true;
+    else if (c.score_path != 1)
+        for (int64_t i = 0; i < C && !b->score64; ++i)
+            if (!score_safe_int32(totalAll, t0s[i], graphs[i]->B)) b->score64 = true;
+
+    // Beta tables over the executed sweeps.
+    BetaTables bt;
+    int rc = build_beta(t0s, C, static_cast<int64_t>(total), bt);
+    if (rc) return rc;
+
+    // Shared memory plan and geometry.
+    b->pmax = static_cast<int>(std::max<uint64_t>(1, std::min<uint64_t>(maxP, std::max(maxN, 1))));
+    b->smem = smem_bytes(std::max(maxN, 1), std::max(maxWords, 1), b->pmax);
+    if (b->smem > static_cast<size_t>(ctx->smemOptin))
+        return fail(RFMF_ERR_CAPACITY,
+                    "chain state needs %zu B of shared memory (n=%d, P=%d) but the device "
+                    "offers %d B per CTA", b->smem, maxN, b->pmax, ctx->smemOptin);
+    rc = autotune(*b, c.threads_per_chain, c.reg_variant - 1, maxN);
+    if (rc) return rc;
+
+    // Per-chain spin words and initial state.
+    b->chainN.resize(C);
+    b->chainWordOff.resize(C + 1);
+    b->chainWordOff[0] = 0;
+    for (int64_t i = 0; i < C; ++i) {
+        b->chainN[i] = graphs[i]->n;
+        b->chainWordOff[i + 1] = b->chainWordOff[i] + (graphs[i]->n + 31) / 32;
+    }
+    b->words = b->chainWordOff[C];
+    std::vector<uint32_t> bits(static_cast<size_t>(std::max<int64_t>(b->words, 1)), 0u);
+    {
+        size_t sp = 0;
+        for (int64_t i = 0; i < C; ++i) {
+            uint32_t* w = bits.data() + b->chainWordOff[i];
+            for (int64_t v = 0; v < b->chainN[i]; ++v, ++sp)
+                if (initial_spins[sp] >= 0) w[v >> 5] |= 1u << (v & 31);
+        }
+    }
+
+    // Device buffers.
+    if ((rc = b->dGraphs.alloc(hg.size() * sizeof(DevGraph)))) return rc;
+    if ((rc = b->dScheds.alloc(sizeof(DevSchedule)))) return rc;
+    if ((rc = b->dChains.alloc(C * sizeof(DevChain)))) return rc;
+    if ((rc = b->dOrder.alloc(C * sizeof(int32_t)))) return rc;
+    if ((rc = b->dPhaseP.alloc(std::max<int64_t>(nphases, 1) * sizeof(uint32_t)))) return rc;
+    if ((rc = b->dPhaseIters.alloc(std::max<int64_t>(nphases, 1) * sizeof(uint64_t)))) return rc;
+    if ((rc = b->dBetaEnd.alloc(bt.end.size() * sizeof(int64_t)))) return rc;
+    if ((rc = b->dBetaVal.alloc(bt.val.size() * sizeof(int32_t)))) return rc;
+    if ((rc = b->dBits.alloc(bits.size() * sizeof(uint32_t)))) return rc;
+    if ((rc = b->dBest.alloc(bits.size() * sizeof(uint32_t)))) return rc;
+    if ((rc = b->dCtl.alloc(4 * sizeof(int32_t)))) return rc;
+
+    std::vector<uint32_t> hp(std::max<int64_t>(nphases, 1), 0);
+    std::vector<uint64_t> hi(std::max<int64_t>(nphases, 1), 0);
+    for (int64_t p = 0; p < nphases; ++p) { hp[p] = static_cast<uint32_t>(phases[p]); hi[p] = iters[p]; }
+    DevSchedule hs{b->dPhaseP.as<uint32_t>(), b->dPhaseIters.as<uint64_t>(),
+                   static_cast<int32_t>(nphases), 0};
+    std::vector<DevChain> hc(C);
+    for (int64_t i = 0; i < C; ++i) {
+        DevChain& d = hc[i];
+        d.graph = static_cast<int32_t>(b->graphOfChain[i]);
+        d.sched = 0;
+        d.solverSeed = solver_seeds[i];
+        d.betaEnd = b->dBetaEnd.as<int64_t>() + bt.chainOff[i];
+        d.betaVal = b->dBetaVal.as<int32_t>() + bt.chainOff[i];
+        d.betaRuns = bt.chainRuns[i];
+        d.spinBits = b->dBits.as<uint32_t>() + b->chainWordOff[i];
+        d.bestBits = b->dBest.as<uint32_t>() + b->chainWordOff[i];
+        d.cur = kUnsetCut;
+        d.best = kUnsetCut;
+        d.sweepsDone = 0;
+        d.sweepsTotal = total;
+        d.improvedSweeps = 0;
+    }
+    // Work-queue order: largest graphs first (longest items first).
+    std::vector<int32_t> order(C);
+    for (int64_t i = 0; i < C; ++i) order[i] = static_cast<int32_t>(i);
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t z) {
+        return b->chainN[a] > b->chainN[z];
+    });
+
+    cudaStream_t st = ctx->stream;
+    CU(cudaMemcpyAsync(b->dGraphs.p, hg.data(), hg.size() * sizeof(DevGraph), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(b->dScheds.p, &hs, sizeof hs, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(b->dChains.p, hc.data(), C * sizeof(DevChain), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(b->dOrder.p, order.data(), C * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(b->dPhaseP.p, hp.data(), hp.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(b->dPhaseIters.p, hi.data(), hi.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(b->dBetaEnd.p, bt.end.data(), bt.end.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(b->dBetaVal.p, bt.val.data(), bt.val.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(b->dBits.p, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(b->dBest.p, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(b->dCtl.p, 0, 4 * sizeof(int32_t), st));
+    CU(cudaStreamSynchronize(st));
+
+    DevLaunch& L = b->L;
+    L.graphs = b->dGraphs.as<DevGraph>();
+    L.scheds = b->dScheds.as<DevSchedule>();
+    L.chains = b->dChains.as<DevChain>();
+    L.order = b->dOrder.as<int32_t>();
+    L.nchains = static_cast<int32_t>(C);
+    L.ngraphs = static_cast<int32_t>(hg.size());
+    L.nscheds = 1;
+    L.maxP = b->pmax;
+    L.maxWords = std::max(maxWords, 1);
+    L.maxN = std::max(maxN, 1);
+    L.queue = b->dCtl.as<int32_t>();
+    L.error = b->dCtl.as<int32_t>() + 1;
+    L.errorItem = b->dCtl.as<int32_t>() + 2;
+    L.window = 0;
+    std::memcpy(L.lut, ctx->lut, sizeof L.lut);
+    *out = b.release();
+    return RFMF_OK;
+}
+
+namespace {
+int enqueue_run(rfmf_batch* b, uint64_t sweeps) {
+    DevLaunch L = b->L;
+    L.window = sweeps;
+    CU(cudaMemsetAsync(L.queue, 0, sizeof(int32_t), b->ctx->stream));
+    CU(launch_anneal(L, b->score64, b->variant, b->grid, b->threads, b->smem, b->pmax,
+                     b->ctx->stream));
+    return RFMF_OK;
+}
+}  // namespace
+
+extern "C" int rfmf_batch_run(rfmf_batch* b, uint64_t sweeps) {
+    if (!b) return fail(RFMF_ERR_INVALID, "batch is NULL");
+    CU(cudaSetDevice(b->ctx->device));
+    return enqueue_run(b, sweeps);
+}
+
+extern "C" int rfmf_batch_run_graph(rfmf_batch* b, uint64_t sweeps, int launches, int replays) {
+    if (!b || launches <= 0 || replays < 0) return fail(RFMF_ERR_INVALID, "bad arguments");
+    CU(cudaSetDevice(b->ctx->device));
+    if (!b->graphExec || b->graphSweeps != sweeps || b->graphLaunches != launches) {
+        if (b->graphExec) { cudaGraphExecDestroy(b->graphExec); b->graphExec = nullptr; }
+        cudaGraph_t graph = nullptr;
+        CU(cudaStreamBeginCapture(b->ctx->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = RFMF_OK;
+        for (int i = 0; i < launches && rc == RFMF_OK; ++i) rc = enqueue_run(b, sweeps);
+        const cudaError_t ec = cudaStreamEndCapture(b->ctx->stream, &graph);
+        if (rc != RFMF_OK) { if (graph) cudaGraphDestroy(graph); return rc; }
+        if (ec != cudaSuccess) return fail(RFMF_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ec));
+        const cudaError_t ei = cudaGraphInstantiate(&b->graphExec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) { b->graphExec = nullptr; return fail(RFMF_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(ei)); }
+        b->graphSweeps = sweeps;
+        b->graphLaunches = launches;
+    }
+    for (int r = 0; r < replays; ++r) CU(cudaGraphLaunch(b->graphExec, b->ctx->stream));
+    return RFMF_OK;
+}
+
+extern "C" int rfmf_batch_run_timed(rfmf_batch* b, uint64_t sweeps, float* ms) {
+    if (!b || !ms) return fail(RFMF_ERR_INVALID, "batch/ms is NULL");
+    CU(cudaSetDevice(b->ctx->device));
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    int rc = RFMF_OK;
+    if (cudaEventRecord(e0, b->ctx->stream) != cudaSuccess) rc = fail(RFMF_ERR_CUDA, "event record failed");
+    if (!rc) rc = enqueue_run(b, sweeps);
+    if (!rc && cudaEventRecord(e1, b->ctx->stream) != cudaSuccess) rc = fail(RFMF_ERR_CUDA, "event record failed");
+    if (!rc) rc = rfmf_batch_synchronize(b);
+    if (!rc && cudaEventElapsedTime(ms, e0, e1) != cudaSuccess) rc = fail(RFMF_ERR_CUDA, "event elapsed failed");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+extern "C" int rfmf_batch_stats(rfmf_batch* b, uint64_t* improved_sweeps) {
+    if (!b || !improved_sweeps) return fail(RFMF_ERR_INVALID, "batch/out is NULL");
+    CU(cudaSetDevice(b->ctx->device));
+    CU(cudaStreamSynchronize(b->ctx->stream));
+    std::vector<DevChain> hc(b->C);
+    CU(cudaMemcpy(hc.data(), b->dChains.p, b->C * sizeof(DevChain), cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < b->C; ++i) improved_sweeps[i] = hc[i].improvedSweeps;
+    return RFMF_OK;
+}
+
+extern "C" int rfmf_batch_synchronize(rfmf_batch* b) {
+    if (!b) return fail(RFMF_ERR_INVALID, "batch is NULL");
+    CU(cudaSetDevice(b->ctx->device));
+    CU(cudaStreamSynchronize(b->ctx->stream));
+    int32_t ctl[4];
+    CU(cudaMemcpy(ctl, b->dCtl.p, sizeof ctl, cudaMemcpyDeviceToHost));
+    if (ctl[1] != kDevOk) {
+        static const char* names[] = {"ok", "carried cut value disagrees with the spins",
+                                      "beta table shorter than the window", "bad work item"};
+        const int code = ctl[1];
+        return fail(RFMF_ERR_DEVICE, "device error %d (%s) on chain %d", code,
+                    (code >= 0 && code < 4) ? names[code] : "?", ctl[2]);
+    }
+    return RFMF_OK;
+}
+
+extern "C" int rfmf_batch_read(rfmf_batch* b, int8_t* end_spins, int8_t* best_spins,
+                               int64_t* cur_vals, int64_t* best_vals, uint64_t* sweeps_done) {
+    if (!b) return fail(RFMF_ERR_INVALID, "batch is NULL");
+    int rc = rfmf_batch_synchronize(b);
+    if (rc) return rc;
+    std::vector<DevChain> hc(b->C);
+    CU(cudaMemcpy(hc.data(), b->dChains.p, b->C * sizeof(DevChain), cudaMemcpyDeviceToHost));
+    auto unpack = [&](const DevBuf& src, int8_t* dst) -> int {
+        std::vector<uint32_t> w(static_cast<size_t>(std::max<int64_t>(b->words, 1)));
+        CU(cudaMemcpy(w.data(), src.p, w.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        size_t sp = 0;
+        for (int64_t i = 0; i < b->C; ++i) {
+            const uint32_t* cw = w.data() + b->chainWordOff[i];
+            for (int64_t v = 0; v < b->chainN[i]; ++v, ++sp)
+                dst[sp] = ((cw[v >> 5] >> (v & 31)) & 1u) ? 1 : -1;
+        }
+        return RFMF_OK;
+    };
+    if (end_spins && (rc = unpack(b->dBits, end_spins))) return rc;
+    if (best_spins && (rc = unpack(b->dBest, best_spins))) return rc;
+    for (int64_t i = 0; i < b->C; ++i) {
+        if (cur_vals) cur_vals[i] = hc[i].cur;
+        if (best_vals) best_vals[i] = hc[i].best;
+        if (sweeps_done) sweeps_done[i] = hc[i].sweepsDone;
+    }
+    return RFMF_OK;
+}
+
+extern "C" int rfmf_batch_info(const rfmf_batch* b, int64_t* nchains, uint64_t* total_sweeps,
+                               int* threads_per_chain, int* grid, int* score64, int* variant) {
+    if (!b) return fail(RFMF_ERR_INVALID, "batch is NULL");
+    if (nchains) *nchains = b->C;
+    if (total_sweeps) *total_sweeps = b->total;
+    if (threads_per_chain) *threads_per_chain = b->threads;
+    if (grid) *grid = b->grid;
+    if (score64) *score64 = b->score64 ? 1 : 0;
+    if (variant) *variant = b->variant + 1;
+    return RFMF_OK;
+}
+
+extern "C" int rfmf_batch_destroy(rfmf_batch* b) {
+    if (!b) return RFMF_OK;
+    cudaSetDevice(b->ctx->device);
+    delete b;
+    return RFMF_OK;
+}
+
+// ---------------------------------------------------------------- anneal
+extern "C" int rfmf_anneal(rfmf_context* ctx, const rfmf_graph* g, int64_t max_weighted_deg,
+                           int64_t C, const int8_t* initial_spins, const double* t0s,
+                           int64_t nphases, const uint64_t* phases, const uint64_t* iters,
+                           const uint64_t* solver_seeds, const rfmf_launch_config* cfg,
+                           int8_t* end_spins, int8_t* best_spins, float* kernel_ms,
+                           int64_t* kernel_best_vals, int64_t* kernel_final_vals) {
+    if (!ctx || !g) return fail(RFMF_ERR_INVALID, "ctx/graph is NULL");
+    if (C <= 0 || !initial_spins || !t0s || !solver_seeds)
+        return fail(RFMF_ERR_INVALID, "annealGpu needs C > 0 and per-chain arrays");
+    (void)max_weighted_deg;   // the graph carries B; accepted for signature parity
+    const int64_t n = g->n;
+    if (kernel_ms) *kernel_ms = 0.0f;
+    if (n == 0 || nphases == 0) {
+        // src/anneal_kernels.cu:856-868: inputs returned, cutValueCsr values.
+        std::vector<uint32_t> off(n + 1, 0);
+        for (int64_t c = 0; c < C; ++c) {
+            if (end_spins) std::memcpy(end_spins + c * n, initial_spins + c * n, n);
+            if (best_spins) std::memcpy(best_spins + c * n, initial_spins + c * n, n);
+            if (kernel_best_vals) kernel_best_vals[c] = 0;
+            if (kernel_final_vals) kernel_final_vals[c] = 0;
+        }
+        if (n > 0) {
+            // Cut values need the host CSR, which the device graph no longer
+            // has; recompute from the device copy.
+            std::vector<uint32_t> ho(n + 1);
+            std::vector<Edge> he(g->m * 2);
+            CU(cudaMemcpy(ho.data(), g->offsets.p, (n + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            if (!he.empty()) CU(cudaMemcpy(he.data(), g->edges.p, he.size() * sizeof(Edge), cudaMemcpyDeviceToHost));
+            for (int64_t c = 0; c < C; ++c) {
+                int64_t v = 0;
+                const int8_t* s = initial_spins + c * n;
+                for (int64_t x = 0; x < n; ++x)
+                    for (uint32_t i = ho[x]; i < ho[x + 1]; ++i)
+                        if (he[i].col > x && s[x] != s[he[i].col]) v += he[i].w;
+                if (kernel_best_vals) kernel_best_vals[c] = v;
+                if (kernel_final_vals) kernel_final_vals[c] = v;
+            }
+        }
+        return RFMF_OK;
+    }
+    std::vector<const rfmf_graph*> gs(C, g);
+    rfmf_batch* b = nullptr;
+    int rc = rfmf_batch_create(ctx, C, gs.data(), t0s, solver_seeds, initial_spins, nphases,
+                               phases, iters, cfg, &b);
+    if (rc) return rc;
+    std::unique_ptr<rfmf_batch, int (*)(rfmf_batch*)> guard(b, rfmf_batch_destroy);
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    CU(cudaEventRecord(e0, ctx->stream));
+    rc = enqueue_run(b, b->total);
+    if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+    CU(cudaEventRecord(e1, ctx->stream));
+    rc = rfmf_batch_synchronize(b);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (kernel_ms) *kernel_ms = ms;
+    return rfmf_batch_read(b, end_spins, best_spins, kernel_final_vals, kernel_best_vals, nullptr);
+}

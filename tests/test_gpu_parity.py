@@ -1,0 +1,189 @@
+"""GPU parity: librfmf.so against the oracle, bit for bit.
+
+Every test runs the CUDA path through the C ABI and the oracle (CPU
+restatement of src/anneal_kernels.cu:262-491) on the same seeded inputs and
+requires identical end spins, best spins, final and best cut values.  Integer
+work: the tolerance is zero.
+"""
+import numpy as np
+import pytest
+
+from conftest import chains_for
+
+pytestmark = pytest.mark.gpu
+
+FULL_LADDER = [35.0, 50.0, 70.0, 100.0, 140.0, 200.0, 280.0, 400.0]
+
+
+def assert_same(res, o, label=""):
+    assert np.array_equal(res.final_vals, o["cur_vals"]), f"{label} final vals"
+    assert np.array_equal(res.best_vals, o["best_vals"]), f"{label} best vals"
+    assert np.array_equal(res.end_spins, o["end_spins"]), f"{label} end spins"
+    assert np.array_equal(res.best_spins, o["best_spins"]), f"{label} best spins"
+
+
+def run_pair(rfmf, ctx, oracle, g, seeds, t0s, phases, iters, cfg=None):
+    init, solver = chains_for(g, seeds)
+    dg = rfmf.DeviceGraph(ctx, g)
+    res = rfmf.anneal_gpu(ctx, dg, g.max_weighted_degree(), init, t0s, phases, iters, solver,
+                          cfg)
+    o = oracle.anneal(g, init, t0s, solver, phases, iters)
+    # incremental values vs an independent recompute (test_cut_consistency.sh)
+    for c in range(len(seeds)):
+        assert res.best_vals[c] == g.cut_value(res.best_spins[c])
+        assert res.final_vals[c] == g.cut_value(res.end_spins[c])
+    return res, o
+
+
+def small_graphs(rfmf):
+    rng = np.random.default_rng(5)
+    out = [
+        rfmf.csr_from_edges([0], [1], [1], name="edge"),
+        rfmf.csr_from_edges([0, 1, 2], [1, 2, 0], [1, -2, 3], name="triangle"),
+        rfmf.erdos_renyi(9, 0.5, signed=True, seed=1),
+        rfmf.erdos_renyi(63, 0.2, signed=True, seed=2),
+        rfmf.erdos_renyi(64, 0.1, seed=3),
+        rfmf.erdos_renyi(65, 0.15, signed=True, seed=4),
+        rfmf.torus(5, 6, signed=True, seed=5),
+        rfmf.random_tree(50, seed=6),
+    ]
+    # small integer weights in [-5, 5] \ {0}
+    u = rng.integers(0, 40, 200)
+    v = rng.integers(0, 40, 200)
+    w = rng.integers(1, 6, 200) * np.where(rng.random(200) < 0.5, -1, 1)
+    out.append(rfmf.csr_from_edges(u, v, w, name="weighted40"))
+    return out
+
+
+@pytest.mark.parametrize("phases", [[1], [2], [3], [8, 4, 2, 1], [128, 64, 32, 16, 8, 4, 2, 1],
+                                    [5, 7, 100], [1000], [8, 0, 4]])
+def test_small_graphs_phases(rfmf, ctx, oracle, phases):
+    for g in small_graphs(rfmf):
+        iters = [40] * len(phases)
+        res, o = run_pair(rfmf, ctx, oracle, g, [1, 2, 3], [105.0, 35.0, 0.5], phases, iters)
+        assert_same(res, o, f"{g.name} {phases}")
+
+
+@pytest.mark.parametrize("threads", [32, 64, 128, 256])
+@pytest.mark.parametrize("variant", [1, 2, 3])
+def test_schedule_invariance(rfmf, ctx, oracle, threads, variant):
+    """Every launch-geometry knob is output-invariant (the dev tree's knob
+    cross named at tests/test_chain_isolation.sh:29-42)."""
+    g = rfmf.erdos_renyi(300, 0.05, signed=True, seed=11)
+    cfg = rfmf.make_config(threads_per_chain=threads, reg_variant=variant)
+    res, o = run_pair(rfmf, ctx, oracle, g, [7, 8], [70.0, 280.0],
+                      [128, 64, 32, 16, 8, 4, 2, 1], [30] * 8, cfg)
+    assert_same(res, o, f"T={threads} v={variant}")
+
+
+def test_er800_config1_shape(rfmf, ctx, oracle):
+    """ER n=800 p=0.06 +1 weights, the reference's default schedule and t0
+    ladder, 32 chains seeds 0..31 (raw seeds through the API)."""
+    g = rfmf.erdos_renyi(800, 0.06, seed=0)
+    seeds = list(range(32))
+    t0s = [FULL_LADDER[i % 8] for i in range(32)]
+    res, o = run_pair(rfmf, ctx, oracle, g, seeds, t0s, [128, 64, 32, 16, 8, 4, 2, 1],
+                      [250] * 8)
+    assert_same(res, o, "er800")
+
+
+def test_int64_score_path(rfmf, ctx, oracle):
+    """t0 = 0.01 fails the int32 gate (tests/test_chain_isolation.sh:129-131):
+    the whole launch takes the int64 score path."""
+    g = rfmf.erdos_renyi(200, 0.05, seed=12)
+    res, o = run_pair(rfmf, ctx, oracle, g, [42, 42], [0.01, 105.0], [8, 4], [150, 150])
+    assert_same(res, o, "int64 gate")
+    # forcing the int64 path on an int32-safe run changes nothing
+    cfg = rfmf.make_config(score_path=2)
+    res2, o2 = run_pair(rfmf, ctx, oracle, g, [5, 6], [105.0, 35.0], [8, 3, 1], [60, 60, 60],
+                        cfg)
+    assert_same(res2, o2, "forced int64")
+
+
+def test_large_weights(rfmf, ctx, oracle):
+    rng = np.random.default_rng(3)
+    u = rng.integers(0, 150, 900)
+    v = rng.integers(0, 150, 900)
+    w = rng.integers(-100000, 100000, 900)
+    w[w == 0] = 1
+    g = rfmf.csr_from_edges(u, v, w, name="bigw")
+    res, o = run_pair(rfmf, ctx, oracle, g, [1, 2], [105.0, 3.0], [16, 4, 1], [50, 50, 50])
+    assert_same(res, o, "bigw")
+
+
+def test_windows_equal_one_run(rfmf, ctx, oracle):
+    """k sweep batches with device-resident state == one uninterrupted run."""
+    g = rfmf.torus(20, 30, signed=True, seed=7)
+    seeds = [3, 4, 5]
+    init, solver = chains_for(g, seeds)
+    phases, iters = [64, 16, 4, 1], [37, 41, 29, 53]
+    t0s = [100.0, 35.0, 400.0]
+    dg = rfmf.DeviceGraph(ctx, g)
+    b = rfmf.Batch(ctx, [dg] * 3, t0s, solver, list(init), phases, iters)
+    total = sum(iters)
+    done = 0
+    for k in [1, 17, 40, 3, 100, 1000]:
+        b.run(k)
+        done = min(total, done + k)
+    out = b.read()
+    assert all(int(d) == total for d in out["sweeps_done"])
+    o = oracle.anneal(g, init, t0s, solver, phases, iters)
+    for c in range(3):
+        assert np.array_equal(out["end_spins"][c], o["end_spins"][c])
+        assert np.array_equal(out["best_spins"][c], o["best_spins"][c])
+    assert np.array_equal(out["cur_vals"], o["cur_vals"])
+    assert np.array_equal(out["best_vals"], o["best_vals"])
+
+
+def test_multi_graph_batch_isolation(rfmf, ctx, oracle):
+    """Chains over several graphs of uneven size in one persistent launch give
+    the same bytes as each graph alone (tests/test_chain_isolation.sh)."""
+    gs = [rfmf.erdos_renyi(120, 0.1, signed=True, seed=1), rfmf.torus(12, 17, seed=2),
+          rfmf.random_tree(333, signed=True, seed=3), rfmf.planar_like(250, seed=4)]
+    phases, iters = [32, 8, 2, 1], [30, 30, 30, 30]
+    dgs, inits, solvers, t0s, owner = [], [], [], [], []
+    for k, g in enumerate(gs):
+        dg = rfmf.DeviceGraph(ctx, g)
+        for c in range(3):
+            seed = 100 * k + c
+            dgs.append(dg)
+            inits.append(oracle.initial_spins(seed, g.n))
+            solvers.append(rfmf.solver_seed(seed))
+            t0s.append(FULL_LADDER[(k + c) % 8])
+            owner.append(k)
+    b = rfmf.Batch(ctx, dgs, t0s, solvers, inits, phases, iters)
+    b.run(10**9)
+    out = b.read()
+    for i, k in enumerate(owner):
+        g = gs[k]
+        o = oracle.anneal(g, inits[i][None], [t0s[i]], [solvers[i]], phases, iters)
+        assert np.array_equal(out["end_spins"][i], o["end_spins"][0]), i
+        assert np.array_equal(out["best_spins"][i], o["best_spins"][0]), i
+        assert out["best_vals"][i] == o["best_vals"][0]
+        assert out["cur_vals"][i] == o["cur_vals"][0]
+
+
+def test_cuda_graph_replay(rfmf, ctx, oracle):
+    g = rfmf.erdos_renyi_degree(500, 8, signed=True, seed=9)
+    seeds = [11, 12, 13, 14]
+    init, solver = chains_for(g, seeds)
+    phases, iters = [128, 32, 8, 1], [50, 50, 50, 50]
+    t0s = [35.0, 70.0, 140.0, 280.0]
+    dg = rfmf.DeviceGraph(ctx, g)
+    b = rfmf.Batch(ctx, [dg] * 4, t0s, solver, list(init), phases, iters)
+    b.run_graph(25, launches=2, replays=4)   # 8 launches x 25 = 200 sweeps
+    out = b.read()
+    o = oracle.anneal(g, init, t0s, solver, phases, iters)
+    assert np.array_equal(out["best_vals"], o["best_vals"])
+    assert np.array_equal(out["cur_vals"], o["cur_vals"])
+    for c in range(4):
+        assert np.array_equal(out["end_spins"][c], o["end_spins"][c])
+
+
+def test_empty_schedule_returns_inputs(rfmf, ctx):
+    g = rfmf.erdos_renyi(50, 0.2, seed=1)
+    init, solver = chains_for(g, [1, 2])
+    dg = rfmf.DeviceGraph(ctx, g)
+    res = rfmf.anneal_gpu(ctx, dg, g.max_weighted_degree(), init, [105.0, 90.0], [], [], solver)
+    assert np.array_equal(res.end_spins, init) and np.array_equal(res.best_spins, init)
+    assert list(res.best_vals) == [g.cut_value(init[0]), g.cut_value(init[1])]
