@@ -223,7 +223,7 @@ def gpu_arm(args, rank, world):
         sweeps = (sweeps // (8 * K)) * 8 * K
     per_step = sweeps // K
     phases, iters = schedule(sweeps)
-    cfg = R.make_config(threads_per_chain=args.threads, reg_variant=args.variant)
+    cfg = R.make_config(threads_per_chain=args.threads, chains_per_cta=args.chains_per_cta)
     base = rank * args.chains
     setup = chain_setup(graphs, args.chains, base)
 
@@ -320,8 +320,11 @@ def gpu_arm(args, rank, world):
             "phases": PHASES,
             "t0_ladder": LADDER,
             "threads_per_chain": info["threads_per_chain"],
-            "reg_variant": info["reg_variant"],
+            "chains_per_cta": info["chains_per_cta"],
             "grid": info["grid"],
+            "csr": {1: "unit16 in shared memory", 2: "packed32 in shared memory",
+                    3: "HBM"}[info["csr_format"]],
+            "gain_bytes": info["gain_width"],
             "score_path": "int64" if info["score64"] else "int32",
             "l2": "flushed (256 MB write) between timed steps",
             "parallelism": f"replicas x{world}",
@@ -382,7 +385,7 @@ def main():
     ap.add_argument("--sweeps", type=int, default=10_000_000)
     ap.add_argument("--chains", type=int, default=1024)
     ap.add_argument("--threads", type=int, default=0)
-    ap.add_argument("--variant", type=int, default=0)
+    ap.add_argument("--chains-per-cta", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

@@ -111,15 +111,17 @@ int rfmf_beta_tables(const double* t0s, int64_t C, int64_t total_steps,
 /* ---- the annealer ------------------------------------------------------ */
 
 /* Mirrors gpu3::LaunchConfig (src/anneal_gpu.cuh:52-58) plus the knobs the
- * reference fixed in src/tuning.hpp.  Zero-initialise for defaults. */
+ * reference fixed in src/tuning.hpp; every knob is output-invariant.
+ * Zero-initialise for defaults (autotuned). */
 typedef struct rfmf_launch_config {
     int corr;              /* CorrMode; accepted, no effect (FLIP needs no corr walk) */
     int device;            /* informational; the context's device is used */
-    int s_width;           /* 32 or 64; accepted, output-invariant (|D| <= B fits int32) */
-    int threads_per_chain; /* 0 = autotune, else 32, 64, 128 or 256 */
+    int s_width;           /* 32 or 64; accepted (the per-vertex gain width is gain_width) */
+    int threads_per_chain; /* 0 = auto, else 32, 64 or 128 (one chain's warp group) */
     int score_path;        /* 0 = gate (src/host_common.cpp:296-312), 1 = int32, 2 = int64 */
-    int reg_variant;       /* 0 = autotune, 1/2/3 = 128/80/64-register kernel */
-    int reserved[2];
+    int chains_per_cta;    /* 0 = auto, else chains sharing one CTA's copy of the graph */
+    int csr_format;        /* 0 = auto, 1 = unit16 (shared), 2 = packed32 (shared), 3 = HBM */
+    int gain_width;        /* 0 = auto, 1 = int8 (needs B <= 127), 4 = int32 */
 } rfmf_launch_config;
 
 /*
@@ -182,9 +184,21 @@ int rfmf_batch_synchronize(rfmf_batch* b);
 int rfmf_batch_read(rfmf_batch* b, int8_t* end_spins, int8_t* best_spins,
                     int64_t* cur_vals, int64_t* best_vals, uint64_t* sweeps_done);
 
-/* Sweeps of the batch's schedule (sum of iters over phases with P != 0). */
-int rfmf_batch_info(const rfmf_batch* b, int64_t* nchains, uint64_t* total_sweeps,
-                    int* threads_per_chain, int* grid, int* score64, int* reg_variant);
+/* The launch plan the autotuner chose for a batch. */
+typedef struct rfmf_batch_plan {
+    int64_t nchains;
+    uint64_t total_sweeps;     /* sum of iters over phases with P != 0 */
+    int threads_per_chain;
+    int chains_per_cta;
+    int grid;                  /* persistent CTAs per launch */
+    int items;                 /* work items (chain groups) per launch */
+    int score64;               /* 1 if the int64 score path is used */
+    int csr_format;            /* 1 unit16, 2 packed32, 3 HBM */
+    int gain_width;            /* bytes per vertex gain: 1 or 4 */
+    int smem_bytes;            /* dynamic shared memory per CTA */
+} rfmf_batch_plan;
+
+int rfmf_batch_info(const rfmf_batch* b, rfmf_batch_plan* out);
 
 int rfmf_batch_destroy(rfmf_batch* b);
 

@@ -4,7 +4,7 @@ The compute path is librfmf.so (hand-written CUDA + C++ host driver behind the
 C ABI of include/rfmf.h); this package loads it through ctypes and mirrors the
 reference's interface in Python.  There is no CPU fallback.
 """
-from ._lib import LaunchConfig, RfmfError, lib
+from ._lib import BatchPlan, LaunchConfig, RfmfError, lib
 from .api import (SOLVER_SEED_OFFSET, AnnealResult, Batch, Context, DeviceGraph, anneal_gpu,
                   beta_fixed, beta_tables, cut_value, initial_spins, make_config,
                   max_weighted_degree, score_safe_int32, solver_seed, total_steps, version)
@@ -12,7 +12,7 @@ from .graphs import (CsrGraph, csr_from_edges, erdos_renyi, erdos_renyi_degree, 
                      random_tree, read_gset, torus)
 
 __all__ = [
-    "LaunchConfig", "RfmfError", "lib", "SOLVER_SEED_OFFSET", "AnnealResult", "Batch",
+    "BatchPlan", "LaunchConfig", "RfmfError", "lib", "SOLVER_SEED_OFFSET", "AnnealResult", "Batch",
     "Context", "DeviceGraph", "anneal_gpu", "beta_fixed", "beta_tables", "cut_value",
     "initial_spins", "make_config", "max_weighted_degree", "score_safe_int32", "solver_seed",
     "total_steps", "version", "CsrGraph", "csr_from_edges", "erdos_renyi",

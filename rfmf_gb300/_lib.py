@@ -41,7 +41,7 @@ SIGNATURES = [
     ("rfmf_batch_stats", ct.c_int, [_P, _P]),
     ("rfmf_batch_synchronize", ct.c_int, [_P]),
     ("rfmf_batch_read", ct.c_int, [_P, _P, _P, _P, _P, _P]),
-    ("rfmf_batch_info", ct.c_int, [_P, _P, _P, _P, _P, _P, _P]),
+    ("rfmf_batch_info", ct.c_int, [_P, _P]),
     ("rfmf_batch_destroy", ct.c_int, [_P]),
 ]
 
@@ -50,7 +50,16 @@ class LaunchConfig(ct.Structure):
     """rfmf_launch_config (mirrors gpu3::LaunchConfig plus tuning knobs)."""
     _fields_ = [("corr", ct.c_int), ("device", ct.c_int), ("s_width", ct.c_int),
                 ("threads_per_chain", ct.c_int), ("score_path", ct.c_int),
-                ("reg_variant", ct.c_int), ("reserved", ct.c_int * 2)]
+                ("chains_per_cta", ct.c_int), ("csr_format", ct.c_int),
+                ("gain_width", ct.c_int)]
+
+
+class BatchPlan(ct.Structure):
+    """rfmf_batch_plan."""
+    _fields_ = [("nchains", ct.c_int64), ("total_sweeps", ct.c_uint64),
+                ("threads_per_chain", ct.c_int), ("chains_per_cta", ct.c_int),
+                ("grid", ct.c_int), ("items", ct.c_int), ("score64", ct.c_int),
+                ("csr_format", ct.c_int), ("gain_width", ct.c_int), ("smem_bytes", ct.c_int)]
 
 
 STATUS = {0: "RFMF_OK", 1: "RFMF_ERR_INVALID", 2: "RFMF_ERR_CUDA", 3: "RFMF_ERR_NOMEM",

@@ -11,7 +11,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import LaunchConfig, RfmfError, check, lib
+from ._lib import BatchPlan, LaunchConfig, RfmfError, check, lib
 
 # Offset between a chain's raw seed (initial spins) and its Philox solver seed
 # (src/host_common.h:22-25, main.cu:27-29).
@@ -76,15 +76,19 @@ def beta_tables(t0s, total):
     return end, val, off
 
 
-def make_config(threads_per_chain=0, score_path=0, reg_variant=0, corr=0, s_width=32,
-                device=0):
+def make_config(threads_per_chain=0, score_path=0, chains_per_cta=0, csr_format=0,
+                gain_width=0, corr=0, s_width=32, device=0):
+    """rfmf_launch_config; 0 everywhere = autotuned.  csr_format: 1 unit16,
+    2 packed32, 3 HBM; gain_width: 1 (int8) or 4 (int32)."""
     c = LaunchConfig()
     c.corr = corr
     c.device = device
     c.s_width = s_width
     c.threads_per_chain = threads_per_chain
     c.score_path = score_path
-    c.reg_variant = reg_variant
+    c.chains_per_cta = chains_per_cta
+    c.csr_format = csr_format
+    c.gain_width = gain_width
     return c
 
 
@@ -202,12 +206,9 @@ class Batch:
         self.h = h
 
     def info(self):
-        C, tot = ct.c_int64(), ct.c_uint64()
-        th, gr, s64, var = ct.c_int(), ct.c_int(), ct.c_int(), ct.c_int()
-        check(lib().rfmf_batch_info(self.h, ct.byref(C), ct.byref(tot), ct.byref(th),
-                                    ct.byref(gr), ct.byref(s64), ct.byref(var)))
-        return dict(nchains=C.value, total_sweeps=tot.value, threads_per_chain=th.value,
-                    grid=gr.value, score64=bool(s64.value), reg_variant=var.value)
+        p = BatchPlan()
+        check(lib().rfmf_batch_info(self.h, ct.byref(p)))
+        return {name: getattr(p, name) for name, _ in BatchPlan._fields_}
 
     def run(self, sweeps):
         check(lib().rfmf_batch_run(self.h, int(sweeps)))

@@ -1,0 +1,888 @@
+// rfmf_anneal.cu -- the RFMF sweep kernel for GB300 (sm_103a).
+//
+// Method (gt-tinker/rfmf, src/anneal_kernels.cu:262-491): per sweep, every
+// vertex v draws a Q20 Gumbel key from Philox4x32-10 (key = chain seed,
+// counter = (sweep, v>>3)), scores gum + beta*delta(v) with delta(v) the exact
+// cut gain of flipping v, and the best score of each group g = v mod P (ties
+// to the smallest v) wins; the P winners then flip, exactly as if flipped one
+// after another in group order.
+//
+// GB300 design (not the reference's):
+//   * A persistent CTA takes work items of up to K chains of ONE graph.  The
+//     graph's CSR is staged once per item into shared memory by bulk async
+//     copies (cp.async.bulk + mbarrier) in a compact format (2 bytes per entry
+//     for +-1 weights), and K warp groups (W warps each) run K chains side by
+//     side on that one copy.  Chains never synchronise with each other: a
+//     chain's barriers are __syncwarp (W == 1) or a named barrier of its own.
+//   * All mutable chain state stays in shared memory for the whole window:
+//     D[v] = spin[v]*S[v] (the per-vertex gain; int8 with a +128 bias when
+//     the max weighted degree B <= 127, else int32), the spins as bits, and
+//     the best-so-far spins as bits.  Graphs too big for shared memory walk
+//     their CSR in HBM instead (kCsrGlobal); the chain state stays resident.
+//   * SELECT reads only D.  The sweep-uniform part of the Philox counter is
+//     hoisted (rounds 1-3 lose 3 multiplies and 3 xors per block) and two
+//     vertex blocks are in flight per thread.
+//   * The group argmax keeps eight register accumulators per thread (one per
+//     Philox lane j) whenever every thread's lane j lands in one group, folds
+//     them with warp shuffles, and stores one packed (biased score, ~v) key
+//     per group; other P fall back to shared-memory atomics.
+//   * FLIP has no winner-winner correction walk.  With D kept per vertex,
+//     negating the winners' D and scattering 2*w*s_b*s_x into D[x] over the
+//     winners' rows leaves every winner holding D_final, and the cut gain of
+//     the whole flip set is exactly (sum delta_pre - sum D_final) / 2: the
+//     same integer the reference's corr[] formulation (src/anneal_kernels.cu:
+//     133-192, 420-440) adds up.  Row walks issue their loads four at a time.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdint>
+#include <type_traits>
+
+#include "rfmf_device.h"
+
+namespace rfmf {
+
+namespace {
+
+// Published Philox4x32 constants (Salmon et al. 2011).
+constexpr uint32_t kM0 = 0xD2511F53u;
+constexpr uint32_t kM1 = 0xCD9E8D57u;
+constexpr uint32_t kW0 = 0x9E3779B9u;
+constexpr uint32_t kW1 = 0xBB67AE85u;
+
+// Bound on mbarrier polls while a CSR bulk copy lands (each poll may suspend
+// the thread for a hardware-chosen interval); past it the CTA stops taking
+// work and the launch reports kDevCopyTimeout.
+constexpr int kMaxCopyPolls = 1 << 22;
+
+__device__ __forceinline__ void mulwide(uint32_t a, uint32_t b, uint32_t& hi, uint32_t& lo) {
+    const uint64_t p = static_cast<uint64_t>(a) * b;
+    hi = static_cast<uint32_t>(p >> 32);
+    lo = static_cast<uint32_t>(p);
+}
+
+// Philox round keys, k0[r] = seed_lo + r*W0, k1[r] = seed_hi + r*W1.
+struct ChainKeys {
+    uint32_t k0[10];
+    uint32_t k1[10];
+};
+
+__device__ __forceinline__ ChainKeys make_keys(uint64_t seed) {
+    ChainKeys k;
+    uint32_t a = static_cast<uint32_t>(seed), b = static_cast<uint32_t>(seed >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        k.k0[r] = a;
+        k.k1[r] = b;
+        a += kW0;
+        b += kW1;
+    }
+    return k;
+}
+
+// Per-sweep constants.  The Philox counter is (step_lo, step_hi, b, 0): words
+// 0, 1 and 3 are the same for every vertex block of a sweep.
+struct SweepConst {
+    uint32_t A;   // round-1 xor for word 0:  step_hi ^ k0[0]
+    uint32_t Cc;  // round-2 xor for word 0:  hi(M1 * w2_r1) ^ k0[1]
+    uint32_t Dc;  // round-2 xor for word 2:  lo(M0 * step_lo) ^ k1[1]
+    uint32_t E;   // round-3 xor for word 0:  lo(M1 * w2_r1) ^ k0[2]
+};
+
+__device__ __forceinline__ SweepConst make_sweep(uint64_t step, const ChainKeys& k) {
+    const uint32_t slo = static_cast<uint32_t>(step);
+    const uint32_t shi = static_cast<uint32_t>(step >> 32);
+    uint32_t hi0, lo0;
+    mulwide(kM0, slo, hi0, lo0);
+    const uint32_t w2r1 = hi0 ^ k.k1[0];   // counter word 3 (block >> 32) is 0
+    uint32_t hi1, lo1;
+    mulwide(kM1, w2r1, hi1, lo1);
+    SweepConst c;
+    c.A = shi ^ k.k0[0];
+    c.Cc = hi1 ^ k.k0[1];
+    c.Dc = lo0 ^ k.k1[1];
+    c.E = lo1 ^ k.k0[2];
+    return c;
+}
+
+// Philox4x32-10 of counter (step, b, 0) under the chain key; bit-identical to
+// philox4x32_10(gumbelBlockCounter(step, b), key) of src/philox.cuh:77-119.
+__device__ __forceinline__ void philox_block(uint32_t b, const SweepConst& c,
+                                             const ChainKeys& k, uint32_t x[4]) {
+    uint32_t hi, lo;
+    mulwide(kM1, b, hi, lo);                  // round 1
+    uint32_t v0 = hi ^ c.A;
+    uint32_t v1 = lo;
+    mulwide(kM0, v0, hi, lo);                 // round 2
+    v0 = v1 ^ c.Cc;
+    uint32_t v2 = hi ^ c.Dc;
+    uint32_t v3 = lo;
+    uint32_t h0, l0, h1, l1;
+    mulwide(kM0, v0, h0, l0);                 // round 3
+    mulwide(kM1, v2, h1, l1);
+    v0 = h1 ^ c.E;
+    v1 = l1;
+    v2 = h0 ^ v3 ^ k.k1[2];
+    v3 = l0;
+#pragma unroll
+    for (int r = 3; r < 10; ++r) {            // rounds 4..10
+        mulwide(kM0, v0, h0, l0);
+        mulwide(kM1, v2, h1, l1);
+        v0 = h1 ^ v1 ^ k.k0[r];
+        v1 = l1;
+        v2 = h0 ^ v3 ^ k.k1[r];
+        v3 = l0;
+    }
+    x[0] = v0;
+    x[1] = v1;
+    x[2] = v2;
+    x[3] = v3;
+}
+
+// 11-bit field of lane j (src/philox.cuh:121-126).
+__device__ __forceinline__ uint32_t field(const uint32_t x[4], int j) {
+    return ((j & 1) ? (x[j >> 1] >> 16) : x[j >> 1]) & 0x7FFu;
+}
+
+// Packed argmax key [biased score : 32 | ~v : 32]: unsigned order = score
+// order, ties to the smaller v; 0 is the empty slot (src/philox.cuh:128-152).
+__device__ __forceinline__ unsigned long long pack_key(int32_t score, int32_t v) {
+    return (static_cast<unsigned long long>(static_cast<uint32_t>(score) ^ 0x80000000u) << 32) |
+           static_cast<unsigned long long>(~static_cast<uint32_t>(v));
+}
+
+__device__ __forceinline__ int32_t key_vertex(unsigned long long key) {
+    return static_cast<int32_t>(~static_cast<uint32_t>(key));
+}
+
+__device__ __forceinline__ unsigned long long shfl_xor_u64(unsigned long long x, int m) {
+    const uint32_t lo = __shfl_xor_sync(0xFFFFFFFFu, static_cast<uint32_t>(x), m);
+    const uint32_t hi = __shfl_xor_sync(0xFFFFFFFFu, static_cast<uint32_t>(x >> 32), m);
+    return (static_cast<unsigned long long>(hi) << 32) | lo;
+}
+
+__device__ __forceinline__ int spin_of(const uint32_t* bits, int v) {
+    return (bits[v >> 5] >> (v & 31)) & 1;
+}
+
+__device__ __forceinline__ void raise_error(const DevLaunch& L, int code, int item) {
+    if (atomicCAS(L.error, 0, code) == 0) *L.errorItem = item;
+}
+
+// Barrier of one chain's warp group: __syncwarp for one warp, else named
+// barrier grp+1 over the group's 32W threads (barrier 0 is __syncthreads).
+__device__ __forceinline__ void group_sync(int grp, int T) {
+    if (T == 32) {
+        __syncwarp();
+    } else {
+        asm volatile("bar.sync %0, %1;" ::"r"(grp + 1), "r"(T) : "memory");
+    }
+}
+
+// ------------------------------------------------------------ D storage
+// int32 gains: plain words.
+struct D32 {
+    __device__ static __forceinline__ void load8(const unsigned char* D, int b, int32_t d[8]) {
+        const int4 a = *reinterpret_cast<const int4*>(D + 32 * b);
+        const int4 c = *reinterpret_cast<const int4*>(D + 32 * b + 16);
+        d[0] = a.x; d[1] = a.y; d[2] = a.z; d[3] = a.w;
+        d[4] = c.x; d[5] = c.y; d[6] = c.z; d[7] = c.w;
+    }
+    __device__ static __forceinline__ int32_t get(const unsigned char* D, int v) {
+        return reinterpret_cast<const int32_t*>(D)[v];
+    }
+    __device__ static __forceinline__ void set(unsigned char* D, int v, int32_t d) {
+        reinterpret_cast<int32_t*>(D)[v] = d;
+    }
+    __device__ static __forceinline__ void add(unsigned char* D, int v, int32_t delta) {
+        atomicAdd(reinterpret_cast<int*>(D) + v, delta);
+    }
+};
+
+// int8 gains stored as D + 128 in [1, 255] (|D| <= B <= 127).  Every partial
+// sum during a scatter is the gain of some spin configuration, so it stays in
+// range and a shifted 32-bit atomicAdd on the containing word never carries
+// into the neighbouring byte.  (x ^ 0x80) read as int8 is D.
+// Byte k of x sign-extended to 32 bits: prmt with selector nibbles whose msb
+// requests sign replication (the __byte_perm intrinsic drops that bit).
+template <int k>
+__device__ __forceinline__ int32_t sbyte(uint32_t x) {
+    int32_t r;
+    if constexpr (k == 3) {
+        r = static_cast<int32_t>(x) >> 24;
+    } else {
+        constexpr uint32_t sel = static_cast<uint32_t>(k) | ((8u | k) << 4) | ((8u | k) << 8) |
+                                 ((8u | k) << 12);
+        asm("prmt.b32 %0, %1, 0, %2;" : "=r"(r) : "r"(x), "n"(sel));
+    }
+    return r;
+}
+
+struct D8 {
+    __device__ static __forceinline__ void load8(const unsigned char* D, int b, int32_t d[8]) {
+        const uint2 w = *reinterpret_cast<const uint2*>(D + 8 * b);
+        const uint32_t a = w.x ^ 0x80808080u, c = w.y ^ 0x80808080u;
+        d[0] = sbyte<0>(a);
+        d[1] = sbyte<1>(a);
+        d[2] = sbyte<2>(a);
+        d[3] = sbyte<3>(a);
+        d[4] = sbyte<0>(c);
+        d[5] = sbyte<1>(c);
+        d[6] = sbyte<2>(c);
+        d[7] = sbyte<3>(c);
+    }
+    __device__ static __forceinline__ int32_t get(const unsigned char* D, int v) {
+        return static_cast<int32_t>(static_cast<int8_t>(D[v] ^ 0x80u));
+    }
+    __device__ static __forceinline__ void set(unsigned char* D, int v, int32_t d) {
+        D[v] = static_cast<unsigned char>(d + 128);
+    }
+    __device__ static __forceinline__ void add(unsigned char* D, int v, int32_t delta) {
+        atomicAdd(reinterpret_cast<unsigned int*>(D + (v & ~3)),
+                  static_cast<unsigned int>(delta) << (8 * (v & 3)));
+    }
+};
+
+// ------------------------------------------------------------ CSR access
+struct CsrView {
+    const uint32_t* off;
+    const void* ent;
+};
+
+template <int kFmt>
+struct Csr;
+
+template <>
+struct Csr<kCsrUnit16> {
+    __device__ static __forceinline__ void row(const CsrView& c, int v, uint32_t& lo, uint32_t& hi) {
+        lo = c.off[v];
+        hi = c.off[v + 1];
+    }
+    __device__ static __forceinline__ void entry(const CsrView& c, uint32_t i, int& col, int& w) {
+        const uint32_t e = static_cast<const uint16_t*>(c.ent)[i];
+        col = static_cast<int>(e >> 1);
+        w = 1 - 2 * static_cast<int>(e & 1u);
+    }
+};
+
+template <>
+struct Csr<kCsrPacked32> {
+    __device__ static __forceinline__ void row(const CsrView& c, int v, uint32_t& lo, uint32_t& hi) {
+        lo = c.off[v];
+        hi = c.off[v + 1];
+    }
+    __device__ static __forceinline__ void entry(const CsrView& c, uint32_t i, int& col, int& w) {
+        const uint32_t e = static_cast<const uint32_t*>(c.ent)[i];
+        col = static_cast<int>(e & 0xFFFFu);
+        w = static_cast<int32_t>(e) >> 16;
+    }
+};
+
+template <>
+struct Csr<kCsrGlobal> {
+    __device__ static __forceinline__ void row(const CsrView& c, int v, uint32_t& lo, uint32_t& hi) {
+        lo = __ldg(c.off + v);
+        hi = __ldg(c.off + v + 1);
+    }
+    __device__ static __forceinline__ void entry(const CsrView& c, uint32_t i, int& col, int& w) {
+        const int2 e = __ldg(static_cast<const int2*>(c.ent) + i);
+        col = e.x;
+        w = e.y;
+    }
+};
+
+// ------------------------------------------------------------ chain region
+struct ChainSmem {
+    unsigned char* D;
+    uint32_t* bits;
+    uint32_t* best;
+    unsigned long long* slots;   // int32 mode: packed keys
+    long long* scores;           // int64 mode: max score per group (aliases slots)
+    int32_t* ids;                // int64 mode: winner id per group
+    int32_t* win;                // winners of the current sweep
+    int64_t* red;                // one partial per warp of the group
+};
+
+__device__ __forceinline__ ChainSmem carve_chain(unsigned char* base, const DevLaunch& L,
+                                                 int dbytes) {
+    const ChainLayout c = chain_layout(L.maxN, L.maxWords, L.pmax, L.warpsPerChain, dbytes);
+    ChainSmem s;
+    s.D = base + c.d;
+    s.bits = reinterpret_cast<uint32_t*>(base + c.bits);
+    s.best = reinterpret_cast<uint32_t*>(base + c.best);
+    s.slots = reinterpret_cast<unsigned long long*>(base + c.slots);
+    s.scores = reinterpret_cast<long long*>(base + c.slots);
+    s.ids = reinterpret_cast<int32_t*>(base + c.ids);
+    s.win = reinterpret_cast<int32_t*>(base + c.win);
+    s.red = reinterpret_cast<int64_t*>(base + c.red);
+    return s;
+}
+
+// Exact int64 sum over a chain's warp group; every thread gets the total.
+// (The partials buffer is rewritten only after two more group barriers.)
+__device__ __forceinline__ int64_t group_sum(int64_t v, const ChainSmem& s, int t, int T, int grp) {
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, m);
+    if (T == 32) return v;
+    if ((t & 31) == 0) s.red[t >> 5] = v;
+    group_sync(grp, T);
+    int64_t tot = 0;
+    for (int w = 0; w < (T >> 5); ++w) tot += s.red[w];
+    return tot;
+}
+
+// ---------------------------------------------------------------- SELECT
+// Scores every vertex from pre-sweep D and leaves the winner of every group
+// g < P in the chain's slots (int32 mode: packed key; int64 mode: ids[g]).
+// Slots start each sweep at their empty value (reset by FLIP's reader).
+
+struct Acc32 {
+    int32_t s[8];
+    uint32_t b[8];
+};
+
+__device__ __forceinline__ void score8_32(Acc32& a, const uint32_t x[4], const int32_t d[8],
+                                          int32_t beta, const int32_t* lut, uint32_t b, int lim) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        if (j < lim) {
+            const uint32_t r = field(x, j);
+            const int32_t sc = lut[r & 15u] + static_cast<int32_t>(r >> 4) + beta * d[j];
+            if (sc > a.s[j]) { a.s[j] = sc; a.b[j] = b; }
+        }
+    }
+}
+
+template <class DP>
+__device__ void select32(const ChainSmem& s, const int32_t* lut, int n, int P, int32_t beta,
+                         uint64_t step, const ChainKeys& keys, int t, int T) {
+    const SweepConst sc = make_sweep(step, keys);
+    const int nfull = n >> 3;
+    const bool priv = ((8 * T) % P) == 0;
+    if (priv) {
+        Acc32 a;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) { a.s[j] = INT32_MIN; a.b[j] = 0; }
+        int b = t;
+        for (; b + T < nfull; b += 2 * T) {
+            uint32_t xa[4], xb[4];
+            int32_t da[8], db[8];
+            philox_block(static_cast<uint32_t>(b), sc, keys, xa);
+            philox_block(static_cast<uint32_t>(b + T), sc, keys, xb);
+            DP::load8(s.D, b, da);
+            DP::load8(s.D, b + T, db);
+            score8_32(a, xa, da, beta, lut, static_cast<uint32_t>(b), 8);
+            score8_32(a, xb, db, beta, lut, static_cast<uint32_t>(b + T), 8);
+        }
+        if (b < nfull) {
+            uint32_t xa[4];
+            int32_t da[8];
+            philox_block(static_cast<uint32_t>(b), sc, keys, xa);
+            DP::load8(s.D, b, da);
+            score8_32(a, xa, da, beta, lut, static_cast<uint32_t>(b), 8);
+            b += T;
+        }
+        if ((n & 7) && b == nfull) {
+            uint32_t xa[4];
+            int32_t da[8];
+            philox_block(static_cast<uint32_t>(b), sc, keys, xa);
+            DP::load8(s.D, b, da);
+            score8_32(a, xa, da, beta, lut, static_cast<uint32_t>(b), n & 7);
+        }
+        unsigned long long k[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            k[j] = (a.s[j] == INT32_MIN) ? 0ull
+                                         : pack_key(a.s[j], static_cast<int32_t>(8 * a.b[j] + j));
+        if ((256 % P) == 0) {
+            // Groups repeat with period P inside a warp's 256 vertices: fold
+            // lanes (and, for P < 8, accumulators) that share a group.
+            if (P <= 4) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) if (k[j + 4] > k[j]) k[j] = k[j + 4];
+            }
+            if (P <= 2) {
+#pragma unroll
+                for (int j = 0; j < 2; ++j) if (k[j + 2] > k[j]) k[j] = k[j + 2];
+            }
+            if (P == 1) {
+                if (k[1] > k[0]) k[0] = k[1];
+            }
+            const int period = (P >= 8) ? (P >> 3) : 1;
+#pragma unroll
+            for (int m = 16; m >= 1; m >>= 1) {
+                if (m >= period) {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const unsigned long long o = shfl_xor_u64(k[j], m);
+                        if (o > k[j]) k[j] = o;
+                    }
+                }
+            }
+            const int lane = t & 31;
+            if (lane < period) {
+                const int jn = (P < 8) ? P : 8;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    if (j < jn && k[j]) {
+                        const int g = (8 * lane + j) % P;
+                        if (T == 32) s.slots[g] = k[j];
+                        else atomicMax(&s.slots[g], k[j]);
+                    }
+                }
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (k[j]) atomicMax(&s.slots[(8 * t + j) % P], k[j]);
+        }
+    } else {
+        // General P: one shared atomic per vertex.
+        for (int b = t; 8 * b < n; b += T) {
+            uint32_t x[4];
+            int32_t d[8];
+            philox_block(static_cast<uint32_t>(b), sc, keys, x);
+            DP::load8(s.D, b, d);
+            int g = (8 * b) % P;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int v = 8 * b + j;
+                if (v < n) {
+                    const uint32_t r = field(x, j);
+                    const int32_t sv = lut[r & 15u] + static_cast<int32_t>(r >> 4) + beta * d[j];
+                    atomicMax(&s.slots[g], pack_key(sv, v));
+                }
+                if (++g == P) g = 0;
+            }
+        }
+    }
+}
+
+// int64 scores (the reference's two-pass path, src/anneal_kernels.cu:348-378,
+// taken when annealScoreSafeInt32 fails): max score per group, then the
+// smallest v reaching it.
+struct Acc64 {
+    long long s[8];
+    uint32_t b[8];
+};
+
+__device__ __forceinline__ void score8_64(Acc64& a, const uint32_t x[4], const int32_t d[8],
+                                          int32_t beta, const int32_t* lut, uint32_t b, int lim) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        if (j < lim) {
+            const uint32_t r = field(x, j);
+            const long long sc = static_cast<long long>(lut[r & 15u] + static_cast<int32_t>(r >> 4)) +
+                                 static_cast<long long>(beta) * d[j];
+            if (sc > a.s[j]) { a.s[j] = sc; a.b[j] = b; }
+        }
+    }
+}
+
+template <class DP>
+__device__ void select64(const ChainSmem& s, const int32_t* lut, int n, int P, int32_t beta,
+                         uint64_t step, const ChainKeys& keys, int t, int T, int grp) {
+    const SweepConst sc = make_sweep(step, keys);
+    const bool priv = ((8 * T) % P) == 0;
+    if (priv) {
+        Acc64 a;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) { a.s[j] = LLONG_MIN; a.b[j] = 0; }
+        for (int b = t; 8 * b < n; b += T) {
+            uint32_t x[4];
+            int32_t d[8];
+            philox_block(static_cast<uint32_t>(b), sc, keys, x);
+            DP::load8(s.D, b, d);
+            const int lim = (n - 8 * b < 8) ? (n - 8 * b) : 8;
+            score8_64(a, x, d, beta, lut, static_cast<uint32_t>(b), lim);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (a.s[j] != LLONG_MIN) atomicMax(&s.scores[(8 * t + j) % P], a.s[j]);
+        group_sync(grp, T);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int g = (8 * t + j) % P;
+            if (a.s[j] != LLONG_MIN && a.s[j] == s.scores[g])
+                atomicMin(&s.ids[g], static_cast<int32_t>(8 * a.b[j] + j));
+        }
+    } else {
+        for (int pass = 0; pass < 2; ++pass) {
+            for (int b = t; 8 * b < n; b += T) {
+                uint32_t x[4];
+                int32_t d[8];
+                philox_block(static_cast<uint32_t>(b), sc, keys, x);
+                DP::load8(s.D, b, d);
+                int g = (8 * b) % P;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const int v = 8 * b + j;
+                    if (v < n) {
+                        const uint32_t r = field(x, j);
+                        const long long sv =
+                            static_cast<long long>(lut[r & 15u] + static_cast<int32_t>(r >> 4)) +
+                            static_cast<long long>(beta) * d[j];
+                        if (pass == 0) atomicMax(&s.scores[g], sv);
+                        else if (sv == s.scores[g]) atomicMin(&s.ids[g], v);
+                    }
+                    if (++g == P) g = 0;
+                }
+            }
+            if (pass == 0) group_sync(grp, T);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ chain
+template <class DP, int kFmt, bool kS64>
+__device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView& csr,
+                          const int32_t* lut, int ci, int t, int T, int grp) {
+    DevChain& ch = L.chains[ci];
+    if (ch.sweepsDone >= ch.sweepsTotal && ch.cur != kUnsetCut) return;
+    const DevGraph& g = L.graphs[ch.graph];
+    const DevSchedule sch = L.scheds[ch.sched];
+    const int n = g.n;
+    const int words = g.words;
+
+    // ---- state in: spin bits and best bits; empty group slots
+    const bool fresh = (ch.cur == kUnsetCut);
+    for (int w = t; w < words; w += T) {
+        const uint32_t sb = ch.spinBits[w];
+        s.bits[w] = sb;
+        s.best[w] = fresh ? sb : ch.bestBits[w];
+    }
+    for (int i = t; i < L.pmax; i += T) {
+        s.slots[i] = kS64 ? static_cast<unsigned long long>(LLONG_MIN) : 0ull;
+        s.ids[i] = INT32_MAX;
+    }
+    group_sync(grp, T);
+
+    // ---- D[v] = spin[v] * sum_u w(v,u) spin[u]; padding past n is 0
+    const int nPad = (n + 7) & ~7;
+    int64_t dsum = 0;
+    for (int v = t; v < nPad; v += T) {
+        int32_t d = 0;
+        if (v < n) {
+            uint32_t lo, hi;
+            Csr<kFmt>::row(csr, v, lo, hi);
+            int32_t acc = 0;
+            for (uint32_t i = lo; i < hi; ++i) {
+                int col, w;
+                Csr<kFmt>::entry(csr, i, col, w);
+                acc += spin_of(s.bits, col) ? w : -w;
+            }
+            d = spin_of(s.bits, v) ? acc : -acc;
+            dsum += d;
+        }
+        DP::set(s.D, v, d);
+    }
+    // cut = (sum over directed entries of w - sum_v D[v]) / 4, exactly.
+    const int64_t cutD = (g.wsum2 - group_sum(dsum, s, t, T, grp)) / 4;
+    int64_t cur = ch.cur, best = ch.best;
+    if (fresh) {
+        cur = best = cutD;
+    } else if (cur != cutD) {
+        if (t == 0) raise_error(L, kDevCutMismatch, ci);
+    }
+
+    // ---- window, beta cursor (first run with end > s0), phase cursor
+    const uint64_t s0 = ch.sweepsDone;
+    const uint64_t s1 = (ch.sweepsTotal - s0 > L.window) ? s0 + L.window : ch.sweepsTotal;
+    int64_t run = 0;
+    {
+        int64_t lo = 0, hi = ch.betaRuns;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (static_cast<uint64_t>(ch.betaEnd[mid]) > s0) hi = mid; else lo = mid + 1;
+        }
+        run = lo;
+    }
+    if (s1 > s0 && (run >= ch.betaRuns ||
+                    static_cast<uint64_t>(ch.betaEnd[ch.betaRuns - 1]) < s1)) {
+        if (t == 0) raise_error(L, kDevBetaTable, ci);
+        return;
+    }
+    int p = 0;
+    uint64_t phaseEnd = 0;
+    int P = 1;
+    {
+        uint64_t acc = 0;
+        for (p = 0; p < sch.nphases; ++p) {
+            if (sch.phaseP[p] == 0) continue;
+            if (acc + sch.phaseIters[p] > s0) break;
+            acc += sch.phaseIters[p];
+        }
+        if (p < sch.nphases) {
+            phaseEnd = acc + sch.phaseIters[p];
+            P = static_cast<int>(umin(sch.phaseP[p], static_cast<uint32_t>(n)));
+        }
+    }
+
+    const ChainKeys keys = make_keys(ch.solverSeed);
+    uint64_t betaNext = (s1 > s0) ? static_cast<uint64_t>(ch.betaEnd[run]) : 0;
+    int32_t beta = (s1 > s0) ? ch.betaVal[run] : 0;
+    uint64_t improved = 0;
+    group_sync(grp, T);
+
+    for (uint64_t sw = s0; sw < s1; ++sw) {
+        while (sw >= phaseEnd) {
+            ++p;
+            if (p >= sch.nphases) break;
+            if (sch.phaseP[p] == 0) continue;
+            phaseEnd += sch.phaseIters[p];
+            P = static_cast<int>(umin(sch.phaseP[p], static_cast<uint32_t>(n)));
+        }
+        if (sw >= betaNext) {
+            ++run;
+            betaNext = static_cast<uint64_t>(ch.betaEnd[run]);
+            beta = ch.betaVal[run];
+        }
+        const uint64_t step = sw + 1;   // 1-based sweep id
+
+        if constexpr (kS64) select64<DP>(s, lut, n, P, beta, step, keys, t, T, grp);
+        else select32<DP>(s, lut, n, P, beta, step, keys, t, T);
+        group_sync(grp, T);
+
+        // ---- FLIP 1: winners; negate their gains, flip their spins
+        int64_t loc = 0;
+        for (int gi = t; gi < P; gi += T) {
+            int v;
+            if constexpr (kS64) {
+                const int32_t id = s.ids[gi];
+                v = (id == INT32_MAX) ? -1 : id;
+                s.scores[gi] = LLONG_MIN;
+                s.ids[gi] = INT32_MAX;
+            } else {
+                const unsigned long long k = s.slots[gi];
+                s.slots[gi] = 0ull;
+                v = k ? key_vertex(k) : -1;
+            }
+            s.win[gi] = v;
+            if (v >= 0) {
+                const int32_t d = DP::get(s.D, v);
+                loc += d;
+                DP::set(s.D, v, -d);
+                atomicXor(&s.bits[v >> 5], 1u << (v & 31));
+            }
+        }
+        group_sync(grp, T);
+
+        // ---- FLIP 2: D[x] += 2 w s_b s_x over the winners' rows (new spins);
+        // `lanes` consecutive threads share a row, four entries in flight.
+        {
+            int lanes = 1;
+            while (lanes * 2 * P <= T && lanes < 32) lanes <<= 1;
+            const int sub = t & (lanes - 1);
+            for (int gi = t / lanes; gi < P; gi += T / lanes) {
+                const int v = s.win[gi];
+                if (v < 0) continue;
+                const int sv = spin_of(s.bits, v);
+                uint32_t lo, hi;
+                Csr<kFmt>::row(csr, v, lo, hi);
+                uint32_t i = lo + sub;
+                for (; i + 3 * lanes < hi; i += 4 * lanes) {
+                    int c0, w0, c1, w1, c2, w2, c3, w3;
+                    Csr<kFmt>::entry(csr, i, c0, w0);
+                    Csr<kFmt>::entry(csr, i + lanes, c1, w1);
+                    Csr<kFmt>::entry(csr, i + 2 * lanes, c2, w2);
+                    Csr<kFmt>::entry(csr, i + 3 * lanes, c3, w3);
+                    const int s0b = spin_of(s.bits, c0), s1b = spin_of(s.bits, c1);
+                    const int s2b = spin_of(s.bits, c2), s3b = spin_of(s.bits, c3);
+                    DP::add(s.D, c0, (sv == s0b) ? 2 * w0 : -2 * w0);
+                    DP::add(s.D, c1, (sv == s1b) ? 2 * w1 : -2 * w1);
+                    DP::add(s.D, c2, (sv == s2b) ? 2 * w2 : -2 * w2);
+                    DP::add(s.D, c3, (sv == s3b) ? 2 * w3 : -2 * w3);
+                }
+                for (; i < hi; i += lanes) {
+                    int c0, w0;
+                    Csr<kFmt>::entry(csr, i, c0, w0);
+                    DP::add(s.D, c0, (sv == spin_of(s.bits, c0)) ? 2 * w0 : -2 * w0);
+                }
+            }
+        }
+        group_sync(grp, T);
+
+        // ---- FLIP 3: gain = (sum delta_pre - sum D_final) / 2
+        for (int gi = t; gi < P; gi += T) {
+            const int v = s.win[gi];
+            if (v >= 0) loc -= DP::get(s.D, v);
+        }
+        const int64_t gain = group_sum(loc, s, t, T, grp) / 2;
+        cur += gain;
+        if (cur > best) {
+            best = cur;
+            ++improved;
+            for (int w = t; w < words; w += T) s.best[w] = s.bits[w];
+        }
+    }
+    group_sync(grp, T);
+
+    // ---- state out
+    for (int w = t; w < words; w += T) {
+        ch.spinBits[w] = s.bits[w];
+        ch.bestBits[w] = s.best[w];
+    }
+    if (t == 0) {
+        ch.cur = cur;
+        ch.best = best;
+        ch.sweepsDone = s1;
+        ch.improvedSweeps += improved;
+    }
+}
+
+// ------------------------------------------------------------ bulk copy
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* mbar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(mbar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* mbar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(mbar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Stage graph g's compact CSR into shared memory: thread 0 arms the mbarrier
+// with the byte count and issues the bulk copies (<= 64 KB each); everyone
+// waits on the phase with a bounded poll.  Returns false on timeout.
+__device__ bool stage_csr(const DevGraph& g, unsigned char* dst, uint64_t* mbar, uint32_t& phase) {
+    const uint32_t total = g.offBytes + g.entBytes;
+    if (threadIdx.x == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(mbar, total);
+        const unsigned char* srcs[2] = {reinterpret_cast<const unsigned char*>(g.offsets),
+                                        static_cast<const unsigned char*>(g.compact)};
+        const uint32_t sizes[2] = {g.offBytes, g.entBytes};
+        uint32_t o = 0;
+        for (int k = 0; k < 2; ++k) {
+            for (uint32_t c = 0; c < sizes[k]; c += 65536u) {
+                const uint32_t len = (sizes[k] - c < 65536u) ? (sizes[k] - c) : 65536u;
+                bulk_g2s(dst + o + c, srcs[k] + c, len, mbar);
+            }
+            o += sizes[k];
+        }
+    }
+    bool ok = false;
+    for (int i = 0; i < kMaxCopyPolls && !ok; ++i) ok = mbar_try_wait(mbar, phase);
+    phase ^= 1u;
+    return ok;
+}
+
+// kDBytes: 1 -> D8, 4 -> D32.
+template <int kDBytes, int kFmt, bool kS64>
+__global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) {
+    using DP = typename std::conditional<kDBytes == 1, D8, D32>::type;
+    extern __shared__ __align__(128) unsigned char smem[];
+    int32_t* lut = reinterpret_cast<int32_t*>(smem);                 // 64 B
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + 64);          // 8 B
+    int* sItem = reinterpret_cast<int*>(smem + 80);
+    unsigned char* csrBase = smem + kSmemHeader;
+    unsigned char* chainBase = csrBase + L.csrBytes;
+
+    const int T = 32 * L.warpsPerChain;
+    const int grp = threadIdx.x / T;
+    const int t = threadIdx.x - grp * T;
+    const ChainSmem cs = carve_chain(chainBase + static_cast<size_t>(grp) * L.chainBytes, L, kDBytes);
+
+    if (threadIdx.x < 16) lut[threadIdx.x] = L.lut[threadIdx.x];
+    if (kFmt != kCsrGlobal && threadIdx.x == 0) mbar_init(mbar);
+    __syncthreads();
+
+    uint32_t phase = 0;
+    int loaded = -1;
+    bool dead = false;
+    for (;;) {
+        if (threadIdx.x == 0) *sItem = atomicAdd(L.queue, 1);
+        __syncthreads();
+        const int it = *sItem;
+        if (it >= L.nitems) break;
+        const DevItem item = L.items[it];
+        if (item.graph < 0 || item.graph >= L.ngraphs) {
+            if (threadIdx.x == 0) raise_error(L, kDevBadItem, it);
+            __syncthreads();
+            continue;
+        }
+        const DevGraph& g = L.graphs[item.graph];
+        CsrView csr;
+        if constexpr (kFmt == kCsrGlobal) {
+            csr.off = g.offsets;
+            csr.ent = g.edges;
+        } else {
+            if (item.graph != loaded && !dead) {
+                if (!stage_csr(g, csrBase, mbar, phase)) {
+                    // The copy may still be in flight: this CTA never touches
+                    // the region again; report and keep draining the queue.
+                    dead = true;
+                    if (threadIdx.x == 0) raise_error(L, kDevCopyTimeout, it);
+                }
+                loaded = item.graph;
+            }
+            csr.off = reinterpret_cast<const uint32_t*>(csrBase);
+            csr.ent = csrBase + g.offBytes;
+        }
+        __syncthreads();
+        if (!dead && grp < item.count && grp < L.chainsPerCta)
+            run_chain<DP, kFmt, kS64>(L, cs, csr, lut, L.order[item.first + grp], t, T, grp);
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ host hooks
+// Kernel variants: D width {1, 4} x CSR format {unit16, packed32, global} x
+// score {int32, int64}.
+const void* kernel_ptr(int dbytes, int fmt, bool s64) {
+#define RFMF_K(DB, F, S) reinterpret_cast<const void*>(&rfmf_anneal_kernel<DB, F, S>)
+    if (dbytes == 1) {
+        if (s64) {
+            if (fmt == kCsrUnit16) return RFMF_K(1, kCsrUnit16, true);
+            if (fmt == kCsrPacked32) return RFMF_K(1, kCsrPacked32, true);
+            return RFMF_K(1, kCsrGlobal, true);
+        }
+        if (fmt == kCsrUnit16) return RFMF_K(1, kCsrUnit16, false);
+        if (fmt == kCsrPacked32) return RFMF_K(1, kCsrPacked32, false);
+        return RFMF_K(1, kCsrGlobal, false);
+    }
+    if (s64) {
+        if (fmt == kCsrUnit16) return RFMF_K(4, kCsrUnit16, true);
+        if (fmt == kCsrPacked32) return RFMF_K(4, kCsrPacked32, true);
+        return RFMF_K(4, kCsrGlobal, true);
+    }
+    if (fmt == kCsrUnit16) return RFMF_K(4, kCsrUnit16, false);
+    if (fmt == kCsrPacked32) return RFMF_K(4, kCsrPacked32, false);
+    return RFMF_K(4, kCsrGlobal, false);
+#undef RFMF_K
+}
+
+cudaError_t launch_anneal(const DevLaunch& L, int dbytes, int fmt, bool s64, int grid,
+                          int threads, size_t smem, cudaStream_t stream) {
+    void* args[] = {const_cast<DevLaunch*>(&L)};
+    return cudaLaunchKernel(kernel_ptr(dbytes, fmt, s64), dim3(grid), dim3(threads), args, smem,
+                            stream);
+}
+
+}  // namespace rfmf

@@ -3,8 +3,8 @@
 #ifndef RFMF_DEVICE_H
 #define RFMF_DEVICE_H
 
-#include <cstdint>
 #include <climits>
+#include <cstdint>
 
 namespace rfmf {
 
@@ -14,17 +14,27 @@ struct alignas(8) Edge {
     int32_t w;
 };
 
+// How a launch reads the CSR.  The compact formats are copied once per CTA
+// into shared memory (bulk async copy) and walked there; kCsrGlobal walks the
+// 8-byte entries in HBM through L1/L2 (graphs too large for shared memory).
+enum CsrFormat : int32_t {
+    kCsrUnit16 = 0,    // uint16 entry = (col << 1) | (w < 0); |w| == 1, n <= 32768
+    kCsrPacked32 = 1,  // uint32 entry = (w << 16) | col;  |w| < 2^15, n <= 65536
+    kCsrGlobal = 2,    // Edge {col, w} in HBM
+};
+
 // One CSR graph in HBM, read-only, shared by every chain that anneals it.
 // Rows are sorted ascending by neighbour (the reference's AnnealCsr order,
 // src/immutable_graph.hpp:83-101); each undirected edge is stored twice.
-// An edge is one 8-byte word {col, weight} so a neighbour walk issues one
-// load per entry.
 struct DevGraph {
-    const uint32_t* offsets;   // n + 1
+    const uint32_t* offsets;   // n + 1 (padded to 16 B)
     const Edge*     edges;     // 2m  {col, weight}
+    const void*     compact;   // 2m compact entries of the launch's format (padded to 16 B)
     int32_t         n;
     int32_t         words;     // ceil(n / 32): spin bit-words per chain
     int64_t         wsum2;     // sum of weight over directed entries (2 * sum over edges)
+    uint32_t        offBytes;  // bytes of offsets, multiple of 16
+    uint32_t        entBytes;  // bytes of compact entries, multiple of 16
 };
 
 // One schedule: phases (group counts P) and sweeps per phase, shared by the
@@ -37,9 +47,9 @@ struct DevSchedule {
     int32_t         pad;
 };
 
-// One chain = one work item of the persistent kernel.  The chain's state
-// (spin bits, best-spin bits, current and best cut) lives in HBM between
-// launches and in shared memory while a CTA runs it.
+// One chain.  Its state (spin bits, best-spin bits, current and best cut,
+// progress) lives in HBM between launches and in shared memory while a
+// warp group runs it.
 struct DevChain {
     int32_t         graph;        // index into the graph table
     int32_t         sched;        // index into the schedule table
@@ -56,6 +66,16 @@ struct DevChain {
     uint64_t        improvedSweeps;  // sweeps that raised the best cut (statistic)
 };
 
+// One work item of the persistent kernel: up to K chains of ONE graph, run
+// side by side by the K warp groups of a CTA on one shared-memory copy of
+// the graph.  The chains are order[first .. first + count).
+struct DevItem {
+    int32_t graph;
+    int32_t first;
+    int32_t count;
+    int32_t pad;
+};
+
 // Error word written by the kernel (0 = ok).  The kernel never traps: it
 // records the first problem it sees and lets the CTA finish.
 enum DevError : int32_t {
@@ -63,6 +83,7 @@ enum DevError : int32_t {
     kDevCutMismatch = 1,     // carried cut value disagrees with the spins
     kDevBetaTable = 2,       // beta table shorter than the window
     kDevBadItem = 3,         // graph/schedule index out of range
+    kDevCopyTimeout = 4,     // bulk copy of the CSR did not complete in time
 };
 
 // Launch-wide parameters.
@@ -70,16 +91,21 @@ struct DevLaunch {
     const DevGraph*    graphs;
     const DevSchedule* scheds;
     DevChain*          chains;
-    const int32_t*     order;       // work-queue order (chain indices)
-    int32_t            nchains;
+    const DevItem*     items;
+    const int32_t*     order;       // chain indices grouped by item
+    int32_t            nitems;
     int32_t            ngraphs;
     int32_t            nscheds;
-    int32_t            maxP;        // largest phase P in any schedule of the launch
-    int32_t            maxWords;    // largest spin word count of any graph
-    int32_t            maxN;        // largest n
+    int32_t            warpsPerChain;   // W: threads per chain = 32 W
+    int32_t            chainsPerCta;    // K: warp groups per CTA
+    int32_t            maxN;            // largest n (sizes the per-chain gain array)
+    int32_t            maxWords;        // largest spin word count
+    int32_t            pmax;            // group slots per chain: min(max P, max n)
+    uint32_t           csrBytes;        // shared-memory CSR region (0 for kCsrGlobal)
+    uint32_t           chainBytes;      // shared-memory bytes per chain
     int32_t*           queue;       // work-queue head (zeroed before the launch)
     int32_t*           error;       // first device error (DevError)
-    int32_t*           errorItem;   // chain that raised it
+    int32_t*           errorItem;   // chain/item that raised it
     uint64_t           window;      // sweeps each chain advances in this launch
     int32_t            lut[16];     // Q20 Gumbel quantile table
 };
@@ -87,6 +113,40 @@ struct DevLaunch {
 // cur == kUnsetCut on input: the kernel derives the cut of spinBits itself
 // and starts bestBits/best from it (a fresh chain).
 constexpr int64_t kUnsetCut = INT64_MIN;
+
+// Shared-memory header in front of the CSR region: Gumbel table, bulk-copy
+// mbarrier, work-item slot.
+constexpr uint32_t kSmemHeader = 128;
+
+#if defined(__CUDACC__)
+#define RFMF_HD __host__ __device__ __forceinline__
+#else
+#define RFMF_HD inline
+#endif
+
+RFMF_HD uint32_t align16(uint32_t x) { return (x + 15u) & ~15u; }
+
+// Per-chain shared-memory region, in order: gains D (nPad * dbytes), spin
+// bits, best-spin bits, group key slots (8 B), ids (4 B), winners (4 B),
+// reduction partials (8 B per warp).  Host and kernel both carve with this.
+struct ChainLayout {
+    uint32_t d, bits, best, slots, ids, win, red, total;
+};
+
+RFMF_HD ChainLayout chain_layout(int maxN, int maxWords, int pmax, int warps, int dbytes) {
+    ChainLayout c;
+    const uint32_t nPad = (static_cast<uint32_t>(maxN) + 7u) & ~7u;
+    uint32_t o = 0;
+    c.d = o;     o = align16(o + nPad * static_cast<uint32_t>(dbytes));
+    c.bits = o;  o = align16(o + static_cast<uint32_t>(maxWords) * 4u);
+    c.best = o;  o = align16(o + static_cast<uint32_t>(maxWords) * 4u);
+    c.slots = o; o = align16(o + static_cast<uint32_t>(pmax) * 8u);
+    c.ids = o;   o = align16(o + static_cast<uint32_t>(pmax) * 4u);
+    c.win = o;   o = align16(o + static_cast<uint32_t>(pmax) * 4u);
+    c.red = o;   o = align16(o + static_cast<uint32_t>(warps) * 8u);
+    c.total = o;
+    return c;
+}
 
 }  // namespace rfmf
 

@@ -24,11 +24,9 @@
 #include "rfmf_device.h"
 
 namespace rfmf {
-size_t smem_bytes(int maxN, int maxWords, int pmax);
-const void* kernel_ptr(bool score64, int variant);
-int num_variants();
-cudaError_t launch_anneal(const DevLaunch& L, bool score64, int variant, int grid, int threads,
-                          size_t smem, int pmax, cudaStream_t stream);
+const void* kernel_ptr(int dbytes, int fmt, bool s64);
+cudaError_t launch_anneal(const DevLaunch& L, int dbytes, int fmt, bool s64, int grid,
+                          int threads, size_t smem, cudaStream_t stream);
 }  // namespace rfmf
 
 using namespace rfmf;
@@ -210,10 +208,15 @@ struct rfmf_context {
     int32_t lut[16];
 };
 
+// A graph in device memory: offsets and 8-byte entries for HBM walks, plus
+// the compact entry arrays the shared-memory formats stage from (present
+// when the graph qualifies).  All arrays are padded to 16 bytes.
 struct rfmf_graph {
     rfmf_context* ctx = nullptr;
     int64_t n = 0, m = 0, B = 0, wsum2 = 0;
-    DevBuf offsets, edges;
+    bool unit16 = false, packed32 = false;
+    uint32_t offBytes = 0, u16Bytes = 0, p32Bytes = 0;
+    DevBuf offsets, edges, u16, p32;
 };
 
 struct rfmf_batch {
@@ -221,12 +224,13 @@ struct rfmf_batch {
     int64_t C = 0;
     uint64_t total = 0;
     bool score64 = false;
-    int threads = 0, grid = 0, pmax = 0, variant = 0;
+    int dbytes = 4, fmt = kCsrGlobal, warps = 1, K = 1, threads = 32, grid = 0, pmax = 0;
+    int nitems = 0;
     size_t smem = 0;
     std::vector<int64_t> chainN, chainWordOff;   // per chain
     std::vector<int64_t> graphOfChain;
     int64_t words = 0;                           // total spin words over chains
-    DevBuf dGraphs, dScheds, dChains, dOrder, dPhaseP, dPhaseIters, dBetaEnd, dBetaVal,
+    DevBuf dGraphs, dScheds, dChains, dItems, dOrder, dPhaseP, dPhaseIters, dBetaEnd, dBetaVal,
         dBits, dBest, dCtl;
     DevLaunch L{};
     cudaGraphExec_t graphExec = nullptr;
@@ -377,6 +381,7 @@ extern "C" int rfmf_graph_create(rfmf_context* ctx, int64_t n, const uint32_t* o
     // self loops, symmetric with equal weights (the AnnealCsr invariants the
     // kernel's per-vertex gain bookkeeping relies on).
     int64_t B = 0, wsum2 = 0;
+    bool unit = true, small = true;
     for (int64_t v = 0; v < n; ++v) {
         if (offsets[v + 1] < offsets[v]) return fail(RFMF_ERR_INVALID, "offsets not monotone at %lld", (long long)v);
         int64_t s = 0;
@@ -386,14 +391,16 @@ extern "C" int rfmf_graph_create(rfmf_context* ctx, int64_t n, const uint32_t* o
             if (u == v) return fail(RFMF_ERR_INVALID, "self loop at vertex %lld", (long long)v);
             if (i > offsets[v] && col[i - 1] >= u)
                 return fail(RFMF_ERR_INVALID, "row %lld not strictly ascending", (long long)v);
-            // symmetric entry (u, v) with the same weight
             const int32_t* b = col + offsets[u];
             const int32_t* e = col + offsets[u + 1];
             const int32_t* f = std::lower_bound(b, e, static_cast<int32_t>(v));
             if (f == e || *f != v || weight[f - col] != weight[i])
                 return fail(RFMF_ERR_INVALID, "edge (%lld,%d) has no symmetric twin", (long long)v, u);
+            if (weight[i] == 0) return fail(RFMF_ERR_INVALID, "zero weight on edge (%lld,%d)", (long long)v, u);
             s += std::llabs(static_cast<long long>(weight[i]));
             wsum2 += weight[i];
+            unit = unit && (weight[i] == 1 || weight[i] == -1);
+            small = small && (weight[i] >= -32767 && weight[i] <= 32767);
         }
         B = std::max(B, s);
     }
@@ -407,15 +414,40 @@ extern "C" int rfmf_graph_create(rfmf_context* ctx, int64_t n, const uint32_t* o
     g->m = static_cast<int64_t>(m2 / 2);
     g->B = B;
     g->wsum2 = wsum2;
+    g->unit16 = unit && n <= 32768 && m2 < (uint64_t(1) << 31);
+    g->packed32 = small && n <= 65536 && m2 < (uint64_t(1) << 30);
+    const uint64_t ob = (static_cast<uint64_t>(n + 1) * 4u + 15u) & ~uint64_t(15);
+    g->offBytes = ob > 0xFFFFFFF0ull ? 0xFFFFFFF0u : static_cast<uint32_t>(ob);
+    std::vector<uint32_t> ho(ob / 4, offsets[n]);
+    std::memcpy(ho.data(), offsets, (n + 1) * sizeof(uint32_t));
     std::vector<Edge> he(m2);
     for (uint64_t i = 0; i < m2; ++i) he[i] = Edge{col[i], weight[i]};
-    int rc = g->offsets.alloc((n + 1) * sizeof(uint32_t));
+    int rc = g->offsets.alloc(ob);
     if (rc) return rc;
     rc = g->edges.alloc(m2 * sizeof(Edge));
     if (rc) return rc;
-    CU(cudaMemcpyAsync(g->offsets.p, offsets, (n + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream));
-    if (m2) CU(cudaMemcpyAsync(g->edges.p, he.data(), m2 * sizeof(Edge), cudaMemcpyHostToDevice, ctx->stream));
-    CU(cudaStreamSynchronize(ctx->stream));
+    cudaStream_t st = ctx->stream;
+    CU(cudaMemcpyAsync(g->offsets.p, ho.data(), ob, cudaMemcpyHostToDevice, st));
+    if (m2) CU(cudaMemcpyAsync(g->edges.p, he.data(), m2 * sizeof(Edge), cudaMemcpyHostToDevice, st));
+    std::vector<uint16_t> h16;
+    std::vector<uint32_t> h32;
+    if (g->unit16) {
+        g->u16Bytes = align16(static_cast<uint32_t>(m2 * 2));
+        h16.assign(g->u16Bytes / 2, 0);
+        for (uint64_t i = 0; i < m2; ++i)
+            h16[i] = static_cast<uint16_t>((static_cast<uint32_t>(col[i]) << 1) | (weight[i] < 0 ? 1u : 0u));
+        if ((rc = g->u16.alloc(g->u16Bytes))) return rc;
+        CU(cudaMemcpyAsync(g->u16.p, h16.data(), g->u16Bytes, cudaMemcpyHostToDevice, st));
+    }
+    if (g->packed32) {
+        g->p32Bytes = align16(static_cast<uint32_t>(m2 * 4));
+        h32.assign(g->p32Bytes / 4, 0);
+        for (uint64_t i = 0; i < m2; ++i)
+            h32[i] = (static_cast<uint32_t>(weight[i]) << 16) | static_cast<uint32_t>(col[i]);
+        if ((rc = g->p32.alloc(g->p32Bytes))) return rc;
+        CU(cudaMemcpyAsync(g->p32.p, h32.data(), g->p32Bytes, cudaMemcpyHostToDevice, st));
+    }
+    CU(cudaStreamSynchronize(st));
     *out = g.release();
     return RFMF_OK;
 }
@@ -434,69 +466,114 @@ extern "C" int rfmf_graph_info(const rfmf_graph* g, int64_t* n, int64_t* m, int6
     if (B) *B = g->B;
     return RFMF_OK;
 }
-
 // ------------------------------------------------------------------ batch
 namespace {
 
-// Launch geometry.  Candidates: threads per chain-CTA T in {256..32} (capped
-// so each thread owns at least two Philox blocks of the largest graph) times
-// the register-budget variants (128/80/64 registers).  Preference: every chain
-// resident at once (no tail wave), then the most threads per chain, then the
-// largest register budget.  Grid: every resident CTA slot, up to one per
-// chain (persistent work queue).
-int autotune(rfmf_batch& b, int requestedT, int requestedVariant, int maxN) {
-    const int nv = num_variants();
-    // Every variant may use the device's full opt-in shared memory, so a
-    // launch of any batch stays legal whichever batch set the attribute
-    // last; occupancy below is computed for this batch's actual size.  The
-    // carveout prefers shared memory (chain state) over L1.
-    for (int v = 0; v < nv; ++v) {
-        const void* kern = kernel_ptr(b.score64, v);
-        cudaFuncAttributes fa{};
-        CU(cudaFuncGetAttributes(&fa, kern));
-        const int dynMax = b.ctx->smemOptin - static_cast<int>(fa.sharedSizeBytes);
-        if (static_cast<int>(b.smem) > dynMax)
+// Launch plan: gain width, CSR format, warps per chain W, chains per CTA K.
+//  * gain width: int8 when every graph has B <= 127, else int32;
+//  * CSR format: the most compact shared-memory format every graph supports
+//    (unit16, else packed32), else HBM walks;
+//  * W: one warp per chain unless a chain has enough vertex blocks to keep
+//    more warps busy (about 384 blocks of 8 vertices per extra warp);
+//  * K: the smallest number of chains per CTA that lets every work item be
+//    resident at once (one wave), within shared memory, 512 threads per CTA
+//    and the named-barrier budget; with more chains than that, the largest.
+struct Plan {
+    int dbytes, fmt, warps, K, threads, grid, nitems, pmax;
+    uint32_t csrBytes, chainBytes;
+    size_t smem;
+};
+
+int plan_launch(rfmf_batch& b, const std::vector<const rfmf_graph*>& glist,
+                const std::vector<int64_t>& perGraphChains, int maxN, int maxWords,
+                int64_t maxB, const rfmf_launch_config& c, Plan& pl) {
+    const int sms = b.ctx->sms;
+    pl.pmax = b.pmax;
+    // gain width
+    pl.dbytes = c.gain_width ? c.gain_width : (maxB <= 127 ? 1 : 4);
+    if (pl.dbytes != 1 && pl.dbytes != 4) return fail(RFMF_ERR_INVALID, "gain_width must be 0, 1 or 4");
+    if (pl.dbytes == 1 && maxB > 127)
+        return fail(RFMF_ERR_INVALID, "int8 gains need max weighted degree <= 127 (B=%lld)", (long long)maxB);
+    // CSR format
+    bool allU16 = true, allP32 = true;
+    for (const rfmf_graph* g : glist) { allU16 = allU16 && g->unit16; allP32 = allP32 && g->packed32; }
+    int fmt;
+    if (c.csr_format == 0) fmt = allU16 ? kCsrUnit16 : (allP32 ? kCsrPacked32 : kCsrGlobal);
+    else if (c.csr_format == 1) { if (!allU16) return fail(RFMF_ERR_INVALID, "unit16 CSR needs |w| == 1 and n <= 32768"); fmt = kCsrUnit16; }
+    else if (c.csr_format == 2) { if (!allP32) return fail(RFMF_ERR_INVALID, "packed32 CSR needs |w| < 2^15 and n <= 65536"); fmt = kCsrPacked32; }
+    else if (c.csr_format == 3) fmt = kCsrGlobal;
+    else return fail(RFMF_ERR_INVALID, "csr_format must be 0..3");
+    // warps per chain
+    int W = 1;
+    if (c.threads_per_chain) {
+        if (c.threads_per_chain != 32 && c.threads_per_chain != 64 && c.threads_per_chain != 128)
+            return fail(RFMF_ERR_INVALID, "threads_per_chain must be 0, 32, 64 or 128");
+        W = c.threads_per_chain / 32;
+    } else {
+        const int nblk = (maxN + 7) / 8;
+        while (W < 4 && nblk >= 384 * 2 * W) W *= 2;
+    }
+    const void* kern = kernel_ptr(pl.dbytes, kCsrGlobal, b.score64);
+    cudaFuncAttributes fa{};
+    CU(cudaFuncGetAttributes(&fa, kern));
+    const int64_t dynMax = static_cast<int64_t>(b.ctx->smemOptin) - static_cast<int64_t>(fa.sharedSizeBytes);
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        uint32_t csrBytes = 0;
+        if (fmt != kCsrGlobal)
+            for (const rfmf_graph* g : glist)
+                csrBytes = std::max(csrBytes, g->offBytes + (fmt == kCsrUnit16 ? g->u16Bytes : g->p32Bytes));
+        const uint32_t chainBytes = chain_layout(maxN, maxWords, pl.pmax, W, pl.dbytes).total;
+        const int kCap = std::min(16 / W, W > 1 ? 15 : 16);
+        const int64_t room = dynMax - kSmemHeader - csrBytes;
+        int Kmax = room > 0 ? static_cast<int>(std::min<int64_t>(kCap, room / chainBytes)) : 0;
+        if (c.chains_per_cta) {
+            if (c.chains_per_cta < 1 || c.chains_per_cta > kCap)
+                return fail(RFMF_ERR_INVALID, "chains_per_cta must be 0 or 1..%d", kCap);
+            Kmax = std::min(Kmax, c.chains_per_cta);
+        }
+        if (Kmax < 1) {
+            if (fmt != kCsrGlobal && c.csr_format == 0) { fmt = kCsrGlobal; continue; }
             return fail(RFMF_ERR_CAPACITY,
-                        "chain state needs %zu B of shared memory but %d B are available "
-                        "per CTA", b.smem, dynMax);
-        CU(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dynMax));
-        CU(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                        "one chain needs %u B of shared memory beside a %u B CSR, but a CTA "
+                        "has %lld B", chainBytes, csrBytes, static_cast<long long>(dynMax));
+        }
+        const void* k2 = kernel_ptr(pl.dbytes, fmt, b.score64);
+        CU(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dynMax)));
+        CU(cudaFuncSetAttribute(k2, cudaFuncAttributePreferredSharedMemoryCarveout,
                                 cudaSharedmemCarveoutMaxShared));
-    }
-    auto occ_for = [&](int t, int v) -> int {
-        const void* kern = kernel_ptr(b.score64, v);
-        int occ = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, t, b.smem) != cudaSuccess) {
-            cudaGetLastError();
-            return 0;
-        }
-        return occ;
-    };
-    const int nblk = (maxN + 7) / 8;
-    int tcap = 32;
-    while (tcap * 2 <= 256 && tcap * 2 * 2 <= nblk) tcap *= 2;
-    int bestT = 0, bestV = 0, bestOcc = 0;
-    bool bestAll = false;
-    for (int t = 256; t >= 32; t /= 2) {
-        if (requestedT ? (t != requestedT) : (t > tcap)) continue;
-        for (int v = 0; v < nv; ++v) {
-            if (requestedVariant >= 0 && v != requestedVariant) continue;
-            const int occ = occ_for(t, v);
-            if (occ <= 0) continue;
-            const bool all = static_cast<int64_t>(occ) * b.ctx->sms >= b.C;
-            if (!bestT || (all && !bestAll)) {
-                bestT = t; bestV = v; bestOcc = occ; bestAll = all;
+        auto items_for = [&](int K) {
+            int64_t it = 0;
+            for (int64_t cg : perGraphChains) it += (cg + K - 1) / K;
+            return it;
+        };
+        int bestK = Kmax, bestOcc = 0;
+        for (int K = c.chains_per_cta ? Kmax : 1; K <= Kmax; ++K) {
+            const size_t smem = kSmemHeader + csrBytes + static_cast<size_t>(K) * chainBytes;
+            int occ = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k2, 32 * W * K, smem) != cudaSuccess) {
+                cudaGetLastError();
+                occ = 0;
             }
+            if (occ <= 0) continue;
+            bestK = K;
+            bestOcc = occ;
+            if (items_for(K) <= static_cast<int64_t>(occ) * sms) break;
         }
+        if (bestOcc <= 0)
+            return fail(RFMF_ERR_CAPACITY, "no resident configuration for %u B CSR + %u B per chain",
+                        csrBytes, chainBytes);
+        pl.fmt = fmt;
+        pl.warps = W;
+        pl.K = bestK;
+        pl.threads = 32 * W * bestK;
+        pl.csrBytes = csrBytes;
+        pl.chainBytes = chainBytes;
+        pl.smem = kSmemHeader + csrBytes + static_cast<size_t>(bestK) * chainBytes;
+        pl.nitems = static_cast<int>(items_for(bestK));
+        pl.grid = static_cast<int>(std::min<int64_t>(pl.nitems, static_cast<int64_t>(bestOcc) * sms));
+        return RFMF_OK;
     }
-    if (!bestT)
-        return fail(RFMF_ERR_CAPACITY,
-                    "no resident CTA configuration with %zu B of shared memory "
-                    "(graph too large for shared-memory residency)", b.smem);
-    b.threads = bestT;
-    b.variant = bestV;
-    b.grid = static_cast<int>(std::min<int64_t>(b.C, static_cast<int64_t>(bestOcc) * b.ctx->sms));
-    return RFMF_OK;
+    return fail(RFMF_ERR_CAPACITY, "no launch plan");
 }
 
 }  // namespace
@@ -515,12 +592,7 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
         return fail(RFMF_ERR_INVALID, "bad phases/iters");
     rfmf_launch_config dflt{};
     const rfmf_launch_config& c = cfg ? *cfg : dflt;
-    if (c.threads_per_chain && (c.threads_per_chain != 32 && c.threads_per_chain != 64 &&
-                                c.threads_per_chain != 128 && c.threads_per_chain != 256))
-        return fail(RFMF_ERR_INVALID, "threads_per_chain must be 0, 32, 64, 128 or 256");
-    if (c.reg_variant < 0 || c.reg_variant > num_variants())
-        return fail(RFMF_ERR_INVALID, "register variant must be 0 (auto) or 1..%d", num_variants());
-    const int64_t totalAll = rfmf_total_steps(nphases, iters);   // src/host_common.cpp:196
+    const int64_t totalAll = rfmf_total_steps(nphases, iters);   // src/host_common.cpp:196-210
     if (totalAll < 0) return fail(RFMF_ERR_CAPACITY, "iters total more than 10^12 sweeps");
     uint64_t total = 0, maxP = 0;
     for (int64_t p = 0; p < nphases; ++p) {
@@ -553,16 +625,11 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
         b->graphOfChain[i] = it->second;
     }
     int maxN = 0, maxWords = 0;
-    std::vector<DevGraph> hg(glist.size());
-    for (size_t k = 0; k < glist.size(); ++k) {
-        const rfmf_graph* g = glist[k];
-        hg[k].offsets = g->offsets.as<uint32_t>();
-        hg[k].edges = g->edges.as<Edge>();
-        hg[k].n = static_cast<int32_t>(g->n);
-        hg[k].words = static_cast<int32_t>((g->n + 31) / 32);
-        hg[k].wsum2 = g->wsum2;
-        maxN = std::max<int>(maxN, hg[k].n);
-        maxWords = std::max<int>(maxWords, hg[k].words);
+    int64_t maxB = 0;
+    for (const rfmf_graph* g : glist) {
+        maxN = std::max<int>(maxN, static_cast<int>(g->n));
+        maxWords = std::max<int>(maxWords, static_cast<int>((g->n + 31) / 32));
+        maxB = std::max(maxB, g->B);
     }
 
     // Score path: the reference's gate (src/host_common.cpp:296-312) at each
@@ -578,15 +645,55 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
     int rc = build_beta(t0s, C, static_cast<int64_t>(total), bt);
     if (rc) return rc;
 
-    // Shared memory plan and geometry.
-    b->pmax = static_cast<int>(std::max<uint64_t>(1, std::min<uint64_t>(maxP, std::max(maxN, 1))));
-    b->smem = smem_bytes(std::max(maxN, 1), std::max(maxWords, 1), b->pmax);
-    if (b->smem > static_cast<size_t>(ctx->smemOptin))
-        return fail(RFMF_ERR_CAPACITY,
-                    "chain state needs %zu B of shared memory (n=%d, P=%d) but the device "
-                    "offers %d B per CTA", b->smem, maxN, b->pmax, ctx->smemOptin);
-    rc = autotune(*b, c.threads_per_chain, c.reg_variant - 1, maxN);
+    // Launch plan.
+    b->pmax = static_cast<int>(std::max<uint64_t>(1, std::min<uint64_t>(maxP, static_cast<uint64_t>(maxN))));
+    std::vector<int64_t> perGraph(glist.size(), 0);
+    for (int64_t i = 0; i < C; ++i) ++perGraph[b->graphOfChain[i]];
+    Plan pl{};
+    rc = plan_launch(*b, glist, perGraph, maxN, maxWords, maxB, c, pl);
     if (rc) return rc;
+    b->dbytes = pl.dbytes;
+    b->fmt = pl.fmt;
+    b->warps = pl.warps;
+    b->K = pl.K;
+    b->threads = pl.threads;
+    b->grid = pl.grid;
+    b->nitems = pl.nitems;
+    b->smem = pl.smem;
+
+    std::vector<DevGraph> hg(glist.size());
+    for (size_t k = 0; k < glist.size(); ++k) {
+        const rfmf_graph* g = glist[k];
+        hg[k].offsets = g->offsets.as<uint32_t>();
+        hg[k].edges = g->edges.as<Edge>();
+        hg[k].compact = (pl.fmt == kCsrUnit16) ? g->u16.p : (pl.fmt == kCsrPacked32 ? g->p32.p : nullptr);
+        hg[k].n = static_cast<int32_t>(g->n);
+        hg[k].words = static_cast<int32_t>((g->n + 31) / 32);
+        hg[k].wsum2 = g->wsum2;
+        hg[k].offBytes = g->offBytes;
+        hg[k].entBytes = (pl.fmt == kCsrUnit16) ? g->u16Bytes : (pl.fmt == kCsrPacked32 ? g->p32Bytes : 0);
+    }
+
+    // Work items: graphs largest first, each graph's chains in groups of K.
+    std::vector<int> gorder(glist.size());
+    for (size_t k = 0; k < gorder.size(); ++k) gorder[k] = static_cast<int>(k);
+    std::stable_sort(gorder.begin(), gorder.end(), [&](int a, int z) { return glist[a]->n > glist[z]->n; });
+    std::vector<std::vector<int32_t>> chainsOf(glist.size());
+    for (int64_t i = 0; i < C; ++i) chainsOf[b->graphOfChain[i]].push_back(static_cast<int32_t>(i));
+    std::vector<int32_t> order;
+    std::vector<DevItem> items;
+    order.reserve(C);
+    for (int gk : gorder) {
+        const auto& cl = chainsOf[gk];
+        for (size_t s = 0; s < cl.size(); s += pl.K) {
+            DevItem it{};
+            it.graph = gk;
+            it.first = static_cast<int32_t>(order.size());
+            it.count = static_cast<int32_t>(std::min<size_t>(pl.K, cl.size() - s));
+            for (int q = 0; q < it.count; ++q) order.push_back(cl[s + q]);
+            items.push_back(it);
+        }
+    }
 
     // Per-chain spin words and initial state.
     b->chainN.resize(C);
@@ -611,6 +718,7 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
     if ((rc = b->dGraphs.alloc(hg.size() * sizeof(DevGraph)))) return rc;
     if ((rc = b->dScheds.alloc(sizeof(DevSchedule)))) return rc;
     if ((rc = b->dChains.alloc(C * sizeof(DevChain)))) return rc;
+    if ((rc = b->dItems.alloc(items.size() * sizeof(DevItem)))) return rc;
     if ((rc = b->dOrder.alloc(C * sizeof(int32_t)))) return rc;
     if ((rc = b->dPhaseP.alloc(std::max<int64_t>(nphases, 1) * sizeof(uint32_t)))) return rc;
     if ((rc = b->dPhaseIters.alloc(std::max<int64_t>(nphases, 1) * sizeof(uint64_t)))) return rc;
@@ -642,17 +750,12 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
         d.sweepsTotal = total;
         d.improvedSweeps = 0;
     }
-    // Work-queue order: largest graphs first (longest items first).
-    std::vector<int32_t> order(C);
-    for (int64_t i = 0; i < C; ++i) order[i] = static_cast<int32_t>(i);
-    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t z) {
-        return b->chainN[a] > b->chainN[z];
-    });
 
     cudaStream_t st = ctx->stream;
     CU(cudaMemcpyAsync(b->dGraphs.p, hg.data(), hg.size() * sizeof(DevGraph), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dScheds.p, &hs, sizeof hs, cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dChains.p, hc.data(), C * sizeof(DevChain), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(b->dItems.p, items.data(), items.size() * sizeof(DevItem), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dOrder.p, order.data(), C * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dPhaseP.p, hp.data(), hp.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dPhaseIters.p, hi.data(), hi.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
@@ -667,13 +770,18 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
     L.graphs = b->dGraphs.as<DevGraph>();
     L.scheds = b->dScheds.as<DevSchedule>();
     L.chains = b->dChains.as<DevChain>();
+    L.items = b->dItems.as<DevItem>();
     L.order = b->dOrder.as<int32_t>();
-    L.nchains = static_cast<int32_t>(C);
+    L.nitems = static_cast<int32_t>(items.size());
     L.ngraphs = static_cast<int32_t>(hg.size());
     L.nscheds = 1;
-    L.maxP = b->pmax;
-    L.maxWords = std::max(maxWords, 1);
-    L.maxN = std::max(maxN, 1);
+    L.warpsPerChain = pl.warps;
+    L.chainsPerCta = pl.K;
+    L.maxN = maxN;
+    L.maxWords = maxWords;
+    L.pmax = b->pmax;
+    L.csrBytes = pl.csrBytes;
+    L.chainBytes = pl.chainBytes;
     L.queue = b->dCtl.as<int32_t>();
     L.error = b->dCtl.as<int32_t>() + 1;
     L.errorItem = b->dCtl.as<int32_t>() + 2;
@@ -688,12 +796,11 @@ int enqueue_run(rfmf_batch* b, uint64_t sweeps) {
     DevLaunch L = b->L;
     L.window = sweeps;
     CU(cudaMemsetAsync(L.queue, 0, sizeof(int32_t), b->ctx->stream));
-    CU(launch_anneal(L, b->score64, b->variant, b->grid, b->threads, b->smem, b->pmax,
+    CU(launch_anneal(L, b->dbytes, b->fmt, b->score64, b->grid, b->threads, b->smem,
                      b->ctx->stream));
     return RFMF_OK;
 }
 }  // namespace
-
 extern "C" int rfmf_batch_run(rfmf_batch* b, uint64_t sweeps) {
     if (!b) return fail(RFMF_ERR_INVALID, "batch is NULL");
     CU(cudaSetDevice(b->ctx->device));
@@ -793,15 +900,18 @@ extern "C" int rfmf_batch_read(rfmf_batch* b, int8_t* end_spins, int8_t* best_sp
     return RFMF_OK;
 }
 
-extern "C" int rfmf_batch_info(const rfmf_batch* b, int64_t* nchains, uint64_t* total_sweeps,
-                               int* threads_per_chain, int* grid, int* score64, int* variant) {
-    if (!b) return fail(RFMF_ERR_INVALID, "batch is NULL");
-    if (nchains) *nchains = b->C;
-    if (total_sweeps) *total_sweeps = b->total;
-    if (threads_per_chain) *threads_per_chain = b->threads;
-    if (grid) *grid = b->grid;
-    if (score64) *score64 = b->score64 ? 1 : 0;
-    if (variant) *variant = b->variant + 1;
+extern "C" int rfmf_batch_info(const rfmf_batch* b, rfmf_batch_plan* out) {
+    if (!b || !out) return fail(RFMF_ERR_INVALID, "batch/out is NULL");
+    out->nchains = b->C;
+    out->total_sweeps = b->total;
+    out->threads_per_chain = 32 * b->warps;
+    out->chains_per_cta = b->K;
+    out->grid = b->grid;
+    out->items = b->nitems;
+    out->score64 = b->score64 ? 1 : 0;
+    out->csr_format = b->fmt + 1;
+    out->gain_width = b->dbytes;
+    out->smem_bytes = static_cast<int>(b->smem);
     return RFMF_OK;
 }
 
@@ -875,3 +985,4 @@ extern "C" int rfmf_anneal(rfmf_context* ctx, const rfmf_graph* g, int64_t max_w
     if (kernel_ms) *kernel_ms = ms;
     return rfmf_batch_read(b, end_spins, best_spins, kernel_final_vals, kernel_best_vals, nullptr);
 }
+

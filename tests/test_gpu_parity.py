@@ -64,16 +64,21 @@ def test_small_graphs_phases(rfmf, ctx, oracle, phases):
         assert_same(res, o, f"{g.name} {phases}")
 
 
-@pytest.mark.parametrize("threads", [32, 64, 128, 256])
-@pytest.mark.parametrize("variant", [1, 2, 3])
-def test_schedule_invariance(rfmf, ctx, oracle, threads, variant):
-    """Every launch-geometry knob is output-invariant (the dev tree's knob
-    cross named at tests/test_chain_isolation.sh:29-42)."""
+KNOBS = ([dict(csr_format=f, gain_width=w) for f in (1, 2, 3) for w in (1, 4)] +
+         [dict(threads_per_chain=t) for t in (64, 128)] +
+         [dict(chains_per_cta=k) for k in (1, 5)] +
+         [dict(threads_per_chain=64, chains_per_cta=3, csr_format=3, gain_width=1)])
+
+
+@pytest.mark.parametrize("knobs", KNOBS, ids=lambda k: ",".join(f"{a}={b}" for a, b in k.items()))
+def test_schedule_invariance(rfmf, ctx, oracle, knobs):
+    """Every launch-plan knob is output-invariant (the dev tree's knob cross
+    named at tests/test_chain_isolation.sh:29-42)."""
     g = rfmf.erdos_renyi(300, 0.05, signed=True, seed=11)
-    cfg = rfmf.make_config(threads_per_chain=threads, reg_variant=variant)
-    res, o = run_pair(rfmf, ctx, oracle, g, [7, 8], [70.0, 280.0],
-                      [128, 64, 32, 16, 8, 4, 2, 1], [30] * 8, cfg)
-    assert_same(res, o, f"T={threads} v={variant}")
+    cfg = rfmf.make_config(**knobs)
+    res, o = run_pair(rfmf, ctx, oracle, g, [7, 8, 9], [70.0, 280.0, 35.0],
+                      [128, 64, 32, 16, 8, 4, 2, 1, 3, 100], [30] * 10, cfg)
+    assert_same(res, o, str(knobs))
 
 
 def test_er800_config1_shape(rfmf, ctx, oracle):
