@@ -65,6 +65,11 @@ int rfmf_context_info(const rfmf_context* ctx, int* sm_count, int* smem_optin);
  */
 int rfmf_graph_create(rfmf_context* ctx, int64_t n, const uint32_t* offsets,
                       const int32_t* col, const int32_t* weight, rfmf_graph** out);
+
+/* Host-only check of the invariants rfmf_graph_create requires (no device
+ * work); on success *max_weighted_degree (may be NULL) receives B. */
+int rfmf_csr_validate(int64_t n, const uint32_t* offsets, const int32_t* col,
+                      const int32_t* weight, int64_t* max_weighted_degree);
 int rfmf_graph_destroy(rfmf_graph* g);
 
 /* n, m (undirected edges) and B = max weighted degree; any pointer may be NULL.

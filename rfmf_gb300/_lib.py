@@ -24,6 +24,7 @@ SIGNATURES = [
     ("rfmf_context_info", ct.c_int, [_P, _P, _P]),
     ("rfmf_graph_create", ct.c_int, [_P, _I64, _P, _P, _P, _P]),
     ("rfmf_graph_destroy", ct.c_int, [_P]),
+    ("rfmf_csr_validate", ct.c_int, [_I64, _P, _P, _P, _P]),
     ("rfmf_graph_info", ct.c_int, [_P, _P, _P, _P]),
     ("rfmf_total_steps", _I64, [_I64, _P]),
     ("rfmf_beta_fixed", _I32, [_U64, ct.c_double]),

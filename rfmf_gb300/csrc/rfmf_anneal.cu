@@ -331,6 +331,18 @@ __device__ __forceinline__ int64_t group_sum(int64_t v, const ChainSmem& s, int 
     return tot;
 }
 
+// int32 sum over a chain's warp group with redux.sync (int8 gains: the sums
+// of a sweep's winner gains are bounded by 2 * 127 * P, far inside int32).
+__device__ __forceinline__ int32_t group_sum32(int32_t v, const ChainSmem& s, int t, int T, int grp) {
+    v = __reduce_add_sync(0xFFFFFFFFu, v);
+    if (T == 32) return v;
+    if ((t & 31) == 0) s.red[t >> 5] = v;
+    group_sync(grp, T);
+    int64_t tot = 0;
+    for (int w = 0; w < (T >> 5); ++w) tot += s.red[w];
+    return static_cast<int32_t>(tot);
+}
+
 // ---------------------------------------------------------------- SELECT
 // Scores every vertex from pre-sweep D and leaves the winner of every group
 // g < P in the chain's slots (int32 mode: packed key; int64 mode: ids[g]).
@@ -341,25 +353,76 @@ struct Acc32 {
     uint32_t b[8];
 };
 
+// Branch-free running max with strict improvement: blocks arrive in
+// increasing order, so a tie keeps the earlier (smaller) vertex.
+__device__ __forceinline__ void upd32(Acc32& a, int j, int32_t sc, uint32_t b) {
+    const bool gt = sc > a.s[j];
+    a.b[j] = gt ? b : a.b[j];
+    a.s[j] = max(a.s[j], sc);
+}
+
+// int32 scores, scaled by 16: with r the 11-bit field, f = r and
+// 16*gum = 16*LUT[r & 15] + 16*(r >> 4) = T16[r & 15] + r, where
+// T16[i] = 16*LUT[i] - i.  So 16*score = (16 beta) d + T16[r & 15] + r: an
+// exact scaling (same order, same ties) that needs no separate dither field.
+// The host enables it only when 16 * (betaMax * B + max|gum|) + 2047 < 2^31.
 __device__ __forceinline__ void score8_32(Acc32& a, const uint32_t x[4], const int32_t d[8],
-                                          int32_t beta, const int32_t* lut, uint32_t b, int lim) {
+                                          int32_t beta16, const int32_t* t16, uint32_t b,
+                                          int lim) {
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        if (j < lim) {
-            const uint32_t r = field(x, j);
-            const int32_t sc = lut[r & 15u] + static_cast<int32_t>(r >> 4) + beta * d[j];
-            if (sc > a.s[j]) { a.s[j] = sc; a.b[j] = b; }
-        }
+    for (int w = 0; w < 4; ++w) {
+        const uint32_t f0 = x[w] & 0x7FFu;
+        const uint32_t f1 = (x[w] >> 16) & 0x7FFu;
+        if (2 * w < lim)
+            upd32(a, 2 * w, beta16 * d[2 * w] + t16[f0 & 15u] + static_cast<int32_t>(f0), b);
+        if (2 * w + 1 < lim)
+            upd32(a, 2 * w + 1, beta16 * d[2 * w + 1] + t16[f1 & 15u] + static_cast<int32_t>(f1), b);
     }
 }
 
+// Per-phase constants, recomputed only when P changes (no integer division
+// or modulo by P inside a sweep).
+struct PhaseCfg {
+    int P;
+    int mode;       // 0: P | 256, groups repeat every P/8 lanes (register fold +
+                    //    warp reduction); 1: 8T % P == 0, thread-private groups;
+                    // 2: general P, one shared atomic per vertex
+    int period;     // mode 0: lanes sharing a group (P/8, or 1 for P < 8)
+    int jn;         // mode 0: live accumulators after the fold, min(P, 8)
+    int g0;         // mode 1: (8 t) mod P
+    int laneShift;  // FLIP scatter: log2 of the lanes that share one row
+};
+
+__device__ __forceinline__ PhaseCfg phase_cfg(int P, int t, int T) {
+    PhaseCfg c;
+    c.P = P;
+    c.mode = ((256 % P) == 0) ? 0 : (((8 * T) % P) == 0 ? 1 : 2);
+    c.period = (P >= 8) ? (P >> 3) : 1;
+    c.jn = (P < 8) ? P : 8;
+    c.g0 = (8 * t) % P;
+    int sh = 0;
+    while ((2 << sh) * P <= T && sh < 5) ++sh;
+    c.laneShift = sh;
+    return c;
+}
+
+// Max of a packed key over the full warp with two redux.sync: the max biased
+// score, then the max ~v (smallest v) among the lanes that hold it.
+__device__ __forceinline__ unsigned long long warp_max_key(unsigned long long k) {
+    const uint32_t hi = static_cast<uint32_t>(k >> 32);
+    const uint32_t mhi = __reduce_max_sync(0xFFFFFFFFu, hi);
+    const uint32_t mlo = __reduce_max_sync(0xFFFFFFFFu, hi == mhi ? static_cast<uint32_t>(k) : 0u);
+    return (static_cast<unsigned long long>(mhi) << 32) | mlo;
+}
+
 template <class DP>
-__device__ void select32(const ChainSmem& s, const int32_t* lut, int n, int P, int32_t beta,
-                         uint64_t step, const ChainKeys& keys, int t, int T) {
+__device__ void select32(const ChainSmem& s, const int32_t* t16, int n, const PhaseCfg& pc,
+                         int32_t beta, uint64_t step, const ChainKeys& keys, int t, int T) {
     const SweepConst sc = make_sweep(step, keys);
+    const int32_t beta16 = beta * 16;
     const int nfull = n >> 3;
-    const bool priv = ((8 * T) % P) == 0;
-    if (priv) {
+    const int P = pc.P;
+    if (pc.mode != 2) {
         Acc32 a;
 #pragma unroll
         for (int j = 0; j < 8; ++j) { a.s[j] = INT32_MIN; a.b[j] = 0; }
@@ -371,15 +434,15 @@ __device__ void select32(const ChainSmem& s, const int32_t* lut, int n, int P, i
             philox_block(static_cast<uint32_t>(b + T), sc, keys, xb);
             DP::load8(s.D, b, da);
             DP::load8(s.D, b + T, db);
-            score8_32(a, xa, da, beta, lut, static_cast<uint32_t>(b), 8);
-            score8_32(a, xb, db, beta, lut, static_cast<uint32_t>(b + T), 8);
+            score8_32(a, xa, da, beta16, t16, static_cast<uint32_t>(b), 8);
+            score8_32(a, xb, db, beta16, t16, static_cast<uint32_t>(b + T), 8);
         }
         if (b < nfull) {
             uint32_t xa[4];
             int32_t da[8];
             philox_block(static_cast<uint32_t>(b), sc, keys, xa);
             DP::load8(s.D, b, da);
-            score8_32(a, xa, da, beta, lut, static_cast<uint32_t>(b), 8);
+            score8_32(a, xa, da, beta16, t16, static_cast<uint32_t>(b), 8);
             b += T;
         }
         if ((n & 7) && b == nfull) {
@@ -387,16 +450,16 @@ __device__ void select32(const ChainSmem& s, const int32_t* lut, int n, int P, i
             int32_t da[8];
             philox_block(static_cast<uint32_t>(b), sc, keys, xa);
             DP::load8(s.D, b, da);
-            score8_32(a, xa, da, beta, lut, static_cast<uint32_t>(b), n & 7);
+            score8_32(a, xa, da, beta16, t16, static_cast<uint32_t>(b), n & 7);
         }
         unsigned long long k[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j)
             k[j] = (a.s[j] == INT32_MIN) ? 0ull
                                          : pack_key(a.s[j], static_cast<int32_t>(8 * a.b[j] + j));
-        if ((256 % P) == 0) {
-            // Groups repeat with period P inside a warp's 256 vertices: fold
-            // lanes (and, for P < 8, accumulators) that share a group.
+        if (pc.mode == 0) {
+            // Groups repeat every P/8 lanes inside a warp's 256 vertices:
+            // fold accumulators (P < 8) and lanes that share a group.
             if (P <= 4) {
 #pragma unroll
                 for (int j = 0; j < 4; ++j) if (k[j + 4] > k[j]) k[j] = k[j + 4];
@@ -408,33 +471,41 @@ __device__ void select32(const ChainSmem& s, const int32_t* lut, int n, int P, i
             if (P == 1) {
                 if (k[1] > k[0]) k[0] = k[1];
             }
-            const int period = (P >= 8) ? (P >> 3) : 1;
+            if (P <= 8) {
 #pragma unroll
-            for (int m = 16; m >= 1; m >>= 1) {
-                if (m >= period) {
+                for (int j = 0; j < 8; ++j)
+                    if (j < pc.jn) k[j] = warp_max_key(k[j]);
+            } else {
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        const unsigned long long o = shfl_xor_u64(k[j], m);
-                        if (o > k[j]) k[j] = o;
+                for (int m = 16; m >= 2; m >>= 1) {
+                    if (m >= pc.period) {
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const unsigned long long o = shfl_xor_u64(k[j], m);
+                            if (o > k[j]) k[j] = o;
+                        }
                     }
                 }
             }
             const int lane = t & 31;
-            if (lane < period) {
-                const int jn = (P < 8) ? P : 8;
+            if (lane < pc.period) {
+                // lane < P/8 (or lane 0): group 8*lane + j (or j) is < P.
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
-                    if (j < jn && k[j]) {
-                        const int g = (8 * lane + j) % P;
+                    if (j < pc.jn && k[j]) {
+                        const int g = 8 * lane + j;
                         if (T == 32) s.slots[g] = k[j];
                         else atomicMax(&s.slots[g], k[j]);
                     }
                 }
             }
         } else {
+            int g = pc.g0;
 #pragma unroll
-            for (int j = 0; j < 8; ++j)
-                if (k[j]) atomicMax(&s.slots[(8 * t + j) % P], k[j]);
+            for (int j = 0; j < 8; ++j) {
+                if (k[j]) atomicMax(&s.slots[g], k[j]);
+                if (++g == P) g = 0;
+            }
         }
     } else {
         // General P: one shared atomic per vertex.
@@ -449,7 +520,7 @@ __device__ void select32(const ChainSmem& s, const int32_t* lut, int n, int P, i
                 const int v = 8 * b + j;
                 if (v < n) {
                     const uint32_t r = field(x, j);
-                    const int32_t sv = lut[r & 15u] + static_cast<int32_t>(r >> 4) + beta * d[j];
+                    const int32_t sv = beta16 * d[j] + t16[r & 15u] + static_cast<int32_t>(r);
                     atomicMax(&s.slots[g], pack_key(sv, v));
                 }
                 if (++g == P) g = 0;
@@ -480,10 +551,12 @@ __device__ __forceinline__ void score8_64(Acc64& a, const uint32_t x[4], const i
 }
 
 template <class DP>
-__device__ void select64(const ChainSmem& s, const int32_t* lut, int n, int P, int32_t beta,
-                         uint64_t step, const ChainKeys& keys, int t, int T, int grp) {
+__device__ void select64(const ChainSmem& s, const int32_t* lut, int n, const PhaseCfg& pc,
+                         int32_t beta, uint64_t step, const ChainKeys& keys, int t, int T,
+                         int grp) {
     const SweepConst sc = make_sweep(step, keys);
-    const bool priv = ((8 * T) % P) == 0;
+    const int P = pc.P;
+    const bool priv = pc.mode != 2;
     if (priv) {
         Acc64 a;
 #pragma unroll
@@ -536,7 +609,7 @@ __device__ void select64(const ChainSmem& s, const int32_t* lut, int n, int P, i
 // ------------------------------------------------------------------ chain
 template <class DP, int kFmt, bool kS64>
 __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView& csr,
-                          const int32_t* lut, int ci, int t, int T, int grp) {
+                          const int32_t* lut, const int32_t* t16, int ci, int t, int T, int grp) {
     DevChain& ch = L.chains[ci];
     if (ch.sweepsDone >= ch.sweepsTotal && ch.cur != kUnsetCut) return;
     const DevGraph& g = L.graphs[ch.graph];
@@ -617,6 +690,7 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
             P = static_cast<int>(umin(sch.phaseP[p], static_cast<uint32_t>(n)));
         }
     }
+    PhaseCfg pc = phase_cfg(P, t, T);
 
     const ChainKeys keys = make_keys(ch.solverSeed);
     uint64_t betaNext = (s1 > s0) ? static_cast<uint64_t>(ch.betaEnd[run]) : 0;
@@ -625,12 +699,15 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
     group_sync(grp, T);
 
     for (uint64_t sw = s0; sw < s1; ++sw) {
-        while (sw >= phaseEnd) {
-            ++p;
-            if (p >= sch.nphases) break;
-            if (sch.phaseP[p] == 0) continue;
-            phaseEnd += sch.phaseIters[p];
-            P = static_cast<int>(umin(sch.phaseP[p], static_cast<uint32_t>(n)));
+        if (sw >= phaseEnd) {
+            while (sw >= phaseEnd) {
+                ++p;
+                if (p >= sch.nphases) break;
+                if (sch.phaseP[p] == 0) continue;
+                phaseEnd += sch.phaseIters[p];
+                P = static_cast<int>(umin(sch.phaseP[p], static_cast<uint32_t>(n)));
+            }
+            pc = phase_cfg(P, t, T);
         }
         if (sw >= betaNext) {
             ++run;
@@ -639,12 +716,13 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
         }
         const uint64_t step = sw + 1;   // 1-based sweep id
 
-        if constexpr (kS64) select64<DP>(s, lut, n, P, beta, step, keys, t, T, grp);
-        else select32<DP>(s, lut, n, P, beta, step, keys, t, T);
+        if constexpr (kS64) select64<DP>(s, lut, n, pc, beta, step, keys, t, T, grp);
+        else select32<DP>(s, t16, n, pc, beta, step, keys, t, T);
         group_sync(grp, T);
 
         // ---- FLIP 1: winners; negate their gains, flip their spins
-        int64_t loc = 0;
+        using Loc = typename std::conditional<std::is_same<DP, D8>::value, int32_t, int64_t>::type;
+        Loc loc = 0;
         for (int gi = t; gi < P; gi += T) {
             int v;
             if constexpr (kS64) {
@@ -670,10 +748,9 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
         // ---- FLIP 2: D[x] += 2 w s_b s_x over the winners' rows (new spins);
         // `lanes` consecutive threads share a row, four entries in flight.
         {
-            int lanes = 1;
-            while (lanes * 2 * P <= T && lanes < 32) lanes <<= 1;
+            const int lanes = 1 << pc.laneShift;
             const int sub = t & (lanes - 1);
-            for (int gi = t / lanes; gi < P; gi += T / lanes) {
+            for (int gi = t >> pc.laneShift; gi < P; gi += T >> pc.laneShift) {
                 const int v = s.win[gi];
                 if (v < 0) continue;
                 const int sv = spin_of(s.bits, v);
@@ -707,7 +784,9 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
             const int v = s.win[gi];
             if (v >= 0) loc -= DP::get(s.D, v);
         }
-        const int64_t gain = group_sum(loc, s, t, T, grp) / 2;
+        int64_t gain;
+        if constexpr (std::is_same<DP, D8>::value) gain = group_sum32(loc, s, t, T, grp) / 2;
+        else gain = group_sum(loc, s, t, T, grp) / 2;
         cur += gain;
         if (cur > best) {
             best = cur;
@@ -797,8 +876,9 @@ __global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) 
     using DP = typename std::conditional<kDBytes == 1, D8, D32>::type;
     extern __shared__ __align__(128) unsigned char smem[];
     int32_t* lut = reinterpret_cast<int32_t*>(smem);                 // 64 B
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + 64);          // 8 B
-    int* sItem = reinterpret_cast<int*>(smem + 80);
+    int32_t* t16 = reinterpret_cast<int32_t*>(smem + 64);            // 64 B
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + 128);        // 8 B
+    int* sItem = reinterpret_cast<int*>(smem + 144);
     unsigned char* csrBase = smem + kSmemHeader;
     unsigned char* chainBase = csrBase + L.csrBytes;
 
@@ -807,7 +887,10 @@ __global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) 
     const int t = threadIdx.x - grp * T;
     const ChainSmem cs = carve_chain(chainBase + static_cast<size_t>(grp) * L.chainBytes, L, kDBytes);
 
-    if (threadIdx.x < 16) lut[threadIdx.x] = L.lut[threadIdx.x];
+    if (threadIdx.x < 16) {
+        lut[threadIdx.x] = L.lut[threadIdx.x];
+        t16[threadIdx.x] = 16 * L.lut[threadIdx.x] - static_cast<int32_t>(threadIdx.x);
+    }
     if (kFmt != kCsrGlobal && threadIdx.x == 0) mbar_init(mbar);
     __syncthreads();
 
@@ -845,7 +928,7 @@ __global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) 
         }
         __syncthreads();
         if (!dead && grp < item.count && grp < L.chainsPerCta)
-            run_chain<DP, kFmt, kS64>(L, cs, csr, lut, L.order[item.first + grp], t, T, grp);
+            run_chain<DP, kFmt, kS64>(L, cs, csr, lut, t16, L.order[item.first + grp], t, T, grp);
         __syncthreads();
     }
 }

@@ -114,9 +114,9 @@ struct DevLaunch {
 // and starts bestBits/best from it (a fresh chain).
 constexpr int64_t kUnsetCut = INT64_MIN;
 
-// Shared-memory header in front of the CSR region: Gumbel table, bulk-copy
-// mbarrier, work-item slot.
-constexpr uint32_t kSmemHeader = 128;
+// Shared-memory header in front of the CSR region: Gumbel table (64 B),
+// scaled Gumbel table (64 B), bulk-copy mbarrier, work-item slot.
+constexpr uint32_t kSmemHeader = 256;
 
 #if defined(__CUDACC__)
 #define RFMF_HD __host__ __device__ __forceinline__

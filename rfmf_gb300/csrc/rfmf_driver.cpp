@@ -151,6 +151,16 @@ struct BetaTables {
 };
 
 int build_beta(const double* t0s, int64_t C, int64_t total, BetaTables& bt) {
+    // beta_fixed must stay inside int32: past it the reference's
+    // static_cast<int32_t>(round(...)) (src/host_common.h:73-76) is undefined
+    // behaviour (x86 and Arm even disagree), so such schedules are refused.
+    for (int64_t c = 0; c < C; ++c) {
+        const double bmax = std::round(std::log(1.0 + static_cast<double>(total)) / t0s[c] * 1048576.0);
+        if (!(bmax < 2147483647.0))
+            return fail(RFMF_ERR_INVALID,
+                        "t0=%g over %lld sweeps makes beta_fixed overflow int32", t0s[c],
+                        static_cast<long long>(total));
+    }
     std::vector<double> distinct;
     std::vector<int64_t> first, count;
     bt.chainOff.resize(C);
@@ -178,6 +188,15 @@ bool score_safe_int32(int64_t total, double t0, int64_t B) {
     const int64_t limit = static_cast<int64_t>(std::numeric_limits<int32_t>::max()) - kGumbelMaxMag;
     if (bmf > 0 && B > 0 && B > limit / bmf) return false;
     return (bmf * B + kGumbelMaxMag) < static_cast<int64_t>(std::numeric_limits<int32_t>::max());
+}
+
+// The kernel's int32 path: 16 * (betaMax * B + max|gum|) + 2047 < 2^31,
+// with betaMax = beta_fixed(total) (beta is monotone in the step).
+bool score_safe_int32_scaled(int64_t total, double t0, int64_t B) {
+    const double bmax = std::round(std::log(1.0 + static_cast<double>(std::max<int64_t>(total, 1))) /
+                                   t0 * 1048576.0);
+    return 16.0 * (bmax * static_cast<double>(B) + static_cast<double>(kGumbelMaxMag)) + 2047.0 <
+           2147483647.0;
 }
 
 // Owning device buffer.
@@ -368,20 +387,22 @@ extern "C" int rfmf_beta_tables(const double* t0s, int64_t C, int64_t total_step
 }
 
 // ------------------------------------------------------------------ graph
-extern "C" int rfmf_graph_create(rfmf_context* ctx, int64_t n, const uint32_t* offsets,
-                                 const int32_t* col, const int32_t* weight, rfmf_graph** out) {
-    if (!ctx || !out) return fail(RFMF_ERR_INVALID, "ctx/out is NULL");
-    *out = nullptr;
+namespace {
+struct CsrFacts {
+    int64_t B = 0, wsum2 = 0;
+    bool unit = true, small = true;
+};
+
+// The AnnealCsr invariants the kernel's per-vertex gain bookkeeping relies on
+// (src/immutable_graph.hpp:44-176): monotone offsets, ids in range, rows
+// strictly ascending, no self loops, no zero weights, symmetric with equal
+// weights.
+int validate_csr(int64_t n, const uint32_t* offsets, const int32_t* col, const int32_t* weight,
+                 CsrFacts& f) {
     if (n < 0 || n >= (int64_t(1) << 31)) return fail(RFMF_ERR_INVALID, "n=%lld out of range", (long long)n);
     if (!offsets) return fail(RFMF_ERR_INVALID, "offsets is NULL");
     if (offsets[0] != 0) return fail(RFMF_ERR_INVALID, "offsets[0] must be 0");
-    const uint64_t m2 = offsets[n];
-    if (m2 > 0 && (!col || !weight)) return fail(RFMF_ERR_INVALID, "col/weight is NULL");
-    // Validate: monotone offsets, ids in range, rows strictly ascending, no
-    // self loops, symmetric with equal weights (the AnnealCsr invariants the
-    // kernel's per-vertex gain bookkeeping relies on).
-    int64_t B = 0, wsum2 = 0;
-    bool unit = true, small = true;
+    if (offsets[n] > 0 && (!col || !weight)) return fail(RFMF_ERR_INVALID, "col/weight is NULL");
     for (int64_t v = 0; v < n; ++v) {
         if (offsets[v + 1] < offsets[v]) return fail(RFMF_ERR_INVALID, "offsets not monotone at %lld", (long long)v);
         int64_t s = 0;
@@ -391,21 +412,43 @@ extern "C" int rfmf_graph_create(rfmf_context* ctx, int64_t n, const uint32_t* o
             if (u == v) return fail(RFMF_ERR_INVALID, "self loop at vertex %lld", (long long)v);
             if (i > offsets[v] && col[i - 1] >= u)
                 return fail(RFMF_ERR_INVALID, "row %lld not strictly ascending", (long long)v);
+            if (weight[i] == 0) return fail(RFMF_ERR_INVALID, "zero weight on edge (%lld,%d)", (long long)v, u);
+            if (offsets[u + 1] < offsets[u]) return fail(RFMF_ERR_INVALID, "offsets not monotone at %d", u);
             const int32_t* b = col + offsets[u];
             const int32_t* e = col + offsets[u + 1];
-            const int32_t* f = std::lower_bound(b, e, static_cast<int32_t>(v));
-            if (f == e || *f != v || weight[f - col] != weight[i])
+            const int32_t* q = std::lower_bound(b, e, static_cast<int32_t>(v));
+            if (q == e || *q != v || weight[q - col] != weight[i])
                 return fail(RFMF_ERR_INVALID, "edge (%lld,%d) has no symmetric twin", (long long)v, u);
-            if (weight[i] == 0) return fail(RFMF_ERR_INVALID, "zero weight on edge (%lld,%d)", (long long)v, u);
             s += std::llabs(static_cast<long long>(weight[i]));
-            wsum2 += weight[i];
-            unit = unit && (weight[i] == 1 || weight[i] == -1);
-            small = small && (weight[i] >= -32767 && weight[i] <= 32767);
+            f.wsum2 += weight[i];
+            f.unit = f.unit && (weight[i] == 1 || weight[i] == -1);
+            f.small = f.small && (weight[i] >= -32767 && weight[i] <= 32767);
         }
-        B = std::max(B, s);
+        f.B = std::max(f.B, s);
     }
-    if (B > std::numeric_limits<int32_t>::max())
-        return fail(RFMF_ERR_CAPACITY, "max weighted degree %lld exceeds int32", (long long)B);
+    if (f.B > std::numeric_limits<int32_t>::max())
+        return fail(RFMF_ERR_CAPACITY, "max weighted degree %lld exceeds int32", (long long)f.B);
+    return RFMF_OK;
+}
+}  // namespace
+
+extern "C" int rfmf_csr_validate(int64_t n, const uint32_t* offsets, const int32_t* col,
+                                 const int32_t* weight, int64_t* max_weighted_degree) {
+    CsrFacts f;
+    const int rc = validate_csr(n, offsets, col, weight, f);
+    if (rc == RFMF_OK && max_weighted_degree) *max_weighted_degree = f.B;
+    return rc;
+}
+
+extern "C" int rfmf_graph_create(rfmf_context* ctx, int64_t n, const uint32_t* offsets,
+                                 const int32_t* col, const int32_t* weight, rfmf_graph** out) {
+    if (!ctx || !out) return fail(RFMF_ERR_INVALID, "ctx/out is NULL");
+    *out = nullptr;
+    CsrFacts facts;
+    if (int rc = validate_csr(n, offsets, col, weight, facts)) return rc;
+    const uint64_t m2 = offsets[n];
+    const int64_t B = facts.B, wsum2 = facts.wsum2;
+    const bool unit = facts.unit, small = facts.small;
     CU(cudaSetDevice(ctx->device));
     auto g = std::unique_ptr<rfmf_graph>(new (std::nothrow) rfmf_graph());
     if (!g) return fail(RFMF_ERR_NOMEM, "host allocation failed");
@@ -632,13 +675,20 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
         maxB = std::max(maxB, g->B);
     }
 
-    // Score path: the reference's gate (src/host_common.cpp:296-312) at each
-    // chain's (t0, B); one verdict for the launch.
+    // Score path.  The int32 kernel path scores 16 * (gum + beta * delta)
+    // (exact, see score8_32), so it needs the reference's gate
+    // (src/host_common.cpp:296-312) with 16x headroom at every chain's
+    // (t0, B); otherwise the launch takes the exact int64 path.  Either way
+    // the winners are the reference's.
     b->score64 = false;
     if (c.score_path == 2) b->score64 = true;
-    else if (c.score_path != 1)
+    else {
         for (int64_t i = 0; i < C && !b->score64; ++i)
-            if (!score_safe_int32(totalAll, t0s[i], graphs[i]->B)) b->score64 = true;
+            if (!score_safe_int32_scaled(static_cast<int64_t>(total), t0s[i], graphs[i]->B))
+                b->score64 = true;
+        if (b->score64 && c.score_path == 1)
+            return fail(RFMF_ERR_INVALID, "int32 scores would overflow for this (t0, B, sweeps)");
+    }
 
     // Beta tables over the executed sweeps.
     BetaTables bt;

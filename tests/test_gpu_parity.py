@@ -192,3 +192,27 @@ def test_empty_schedule_returns_inputs(rfmf, ctx):
     res = rfmf.anneal_gpu(ctx, dg, g.max_weighted_degree(), init, [105.0, 90.0], [], [], solver)
     assert np.array_equal(res.end_spins, init) and np.array_equal(res.best_spins, init)
     assert list(res.best_vals) == [g.cut_value(init[0]), g.cut_value(init[1])]
+
+
+def test_golden_anneal_fixtures(rfmf, ctx):
+    """GPU results equal the recorded anneal fixtures (tests/golden/)."""
+    import hashlib
+    import json
+
+    import rfmf_gb300.graphs as G
+    from conftest import GOLDEN
+
+    def psha(s):
+        return hashlib.sha256("".join("0" if x < 0 else "1" for x in s).encode()).hexdigest()
+
+    for case in json.loads((GOLDEN / "anneal_small.json").read_text())["cases"]:
+        fn, kw = case["graph"]
+        g = getattr(G, fn)(**kw)
+        init, solver = chains_for(g, case["seeds"])
+        dg = rfmf.DeviceGraph(ctx, g)
+        res = rfmf.anneal_gpu(ctx, dg, g.max_weighted_degree(), init, case["t0s"],
+                              case["phases"], case["iters"], solver)
+        assert [int(x) for x in res.best_vals] == case["best"]
+        assert [int(x) for x in res.final_vals] == case["final"]
+        assert [psha(x) for x in res.best_spins] == case["best_partition_sha256"]
+        assert [psha(x) for x in res.end_spins] == case["final_partition_sha256"]
