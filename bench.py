@@ -182,7 +182,8 @@ def cpu_rate(graphs, steps, warmup, target_s, rank_seed_base=0):
     ora.anneal(g0, R.initial_spins(1, g0.n)[None], [35.0], [R.solver_seed(1)], PHASES, [40] * 8,
                nthreads=1)
     per_sweep = (time.perf_counter() - t) / 320 * (sum(g.n for g in graphs) / g0.n / len(graphs))
-    sweeps = max(800, int(target_s / max(per_sweep, 1e-7) / 8) * 8)
+    # the two graphs run one after the other, each with one chain per core
+    sweeps = max(800, int(target_s / 2 / max(per_sweep, 1e-7) / 8) * 8)
     nch = max(cores, 2)
     per_graph = [nch // 2, nch - nch // 2]
     rates = []
@@ -338,7 +339,10 @@ def gpu_arm(args, rank, world):
             "peak": smem_peak,
             "unit": "GB/s",
             "frac": achieved / smem_peak,
-            "traffic": (traffic or {}).get("dram_bytes_per_launch_scaled"),
+            "traffic": (traffic or {}).get("dram_bytes_per_launch"),
+            "traffic_note": ("DRAM bytes per launch from profiles/anneal_kernel_traffic.json "
+                             "(ncu, same kernel shape, %s-sweep windows); the working set is "
+                             "shared-memory/L2 resident" % (traffic or {}).get("window_sweeps")),
             "peak_source": f"{sm_count} SMs x 128 B/clk x {sm_mhz:.0f} MHz (median SM clock sampled "
                            "during the timed region)",
             "bytes_model": "5n + min(P,n)(8 + 16 dbar) per chain-sweep + n per improving sweep",
@@ -351,7 +355,7 @@ def gpu_arm(args, rank, world):
 def e2e_arm(args, ctx, graphs, setup, per_step):
     import rfmf_gb300 as R
     phases, iters = schedule(per_step)
-    K = args.steps
+    K = min(args.steps, 2)
     h2d = d2h = 0
     t = time.perf_counter()
     for _ in range(K):
@@ -398,7 +402,7 @@ def main():
         if rank != 0:
             return 0
         graphs = workload_graphs()
-        per_step_s = max(2.0, 150.0 / max(args.steps + args.warmup, 1))
+        per_step_s = max(2.0, 60.0 / max(args.steps + args.warmup, 1))
         rate, cores, sample, el = cpu_rate(graphs, args.steps, args.warmup, per_step_s)
         line = {
             "impl": "reference", "metric": "chain-steps/s", "value": rate,
