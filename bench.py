@@ -292,6 +292,9 @@ def gpu_arm(args, rank, world):
     e2e = None
     if not args.no_e2e:
         e2e = e2e_arm(args, ctx, graphs, setup, per_step)
+    plain = None
+    if not args.no_plain:
+        plain = plain_kernel_arm(graphs, setup, args.plain_sweeps, ctx)
 
     peaks = measured_peaks()
     sm_count = ctx.info()["sm_count"]
@@ -326,12 +329,15 @@ def gpu_arm(args, rank, world):
             "csr": {1: "unit16 in shared memory", 2: "packed32 in shared memory",
                     3: "HBM"}[info["csr_format"]],
             "gain_bytes": info["gain_width"],
+            "items": info["items"],
+            "balanced_items": bool(info["balanced"]),
             "score_path": "int64" if info["score64"] else "int32",
             "l2": "flushed (256 MB write) between timed steps",
             "parallelism": f"replicas x{world}",
         },
         "gpu_launches": K,
         "e2e": e2e,
+        "plain_kernel": plain,
         "clocks": clk,
         "roofline": {
             "bound": "smem",
@@ -350,6 +356,51 @@ def gpu_arm(args, rank, world):
         "wall_s": wall,
     }
     return result
+
+
+def plain_kernel_arm(graphs, setup, sweeps, ctx):
+    """The reference's own kernel (one graph per launch, one block per chain,
+    state in global memory), compiled from its sources for sm_103a and
+    launched through oracle/refgpu.py, on a bounded sample of the same
+    workload; and librfmf.so's annealGpu drop-in on the identical sample."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    try:
+        import refgpu
+    except Exception as e:   # pragma: no cover
+        return {"unavailable": f"harness import failed: {e}"}
+    if not refgpu.available():
+        return {"unavailable": "reference kernel cubin (oracle/_ref) not built on this machine"}
+    import torch
+
+    import rfmf_gb300 as R
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    phases, iters = schedule(sweeps)
+    ref_ms = ours_ms = 0.0
+    cs = 0
+    tpbs = []
+    for s in setup:
+        g = s["g"]
+        r = refgpu.run(g, s["init"], s["t0s"], s["solver"], phases, iters, sms)
+        ref_ms += r["ms"]
+        tpbs.append(r["tpb"])
+        dg = R.DeviceGraph(ctx, g)
+        o = R.anneal_gpu(ctx, dg, g.max_weighted_degree(), s["init"], s["t0s"], phases, iters,
+                         s["solver"])
+        dg.close()
+        ours_ms += o.kernel_ms
+        cs += len(s["seeds"]) * sweeps
+        same = (np.array_equal(o.best_spins, r["best_spins"]) and
+                np.array_equal(o.end_spins, r["end_spins"]) and
+                np.array_equal(o.best_vals, r["best_vals"]))
+        if not same:
+            raise AssertionError(f"reference kernel and librfmf.so differ on {g.name}")
+    return {"value": cs / (ref_ms / 1e3), "unit": "chain-steps/s",
+            "ours_same_sample": cs / (ours_ms / 1e3),
+            "sample": f"{len(setup)} launches (one per graph) x {len(setup[0]['seeds'])} chains x "
+                      f"{sweeps} sweeps (phases 128..1), threads/block {tpbs}",
+            "identical_results": True,
+            "what": "reference mcKernel compiled from its sources for sm_103a, kernel-only "
+                    "cudaEvent time, one graph per launch as the reference runs"}
 
 
 def e2e_arm(args, ctx, graphs, setup, per_step):
@@ -391,6 +442,8 @@ def main():
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--chains-per-cta", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--plain-sweeps", type=int, default=16000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     args = ap.parse_args()

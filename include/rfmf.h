@@ -165,7 +165,9 @@ int rfmf_batch_create(rfmf_context* ctx, int64_t nchains, const rfmf_graph* cons
                       const rfmf_launch_config* cfg, rfmf_batch** out);
 
 /* Enqueue one launch advancing every unfinished chain by up to `sweeps`
- * sweeps, on the context stream; returns without waiting. */
+ * sweeps, on the context stream; returns without waiting.  Work items are
+ * re-sized between launches from the per-graph costs the library learns
+ * from earlier launches' timings (output-invariant). */
 int rfmf_batch_run(rfmf_batch* b, uint64_t sweeps);
 
 /* Capture `launches` rfmf_batch_run(b, sweeps) steps in a CUDA graph and
@@ -201,6 +203,7 @@ typedef struct rfmf_batch_plan {
     int csr_format;            /* 1 unit16, 2 packed32, 3 HBM */
     int gain_width;            /* bytes per vertex gain: 1 or 4 */
     int smem_bytes;            /* dynamic shared memory per CTA */
+    int balanced;              /* 1 once work items are sized from learned graph costs */
 } rfmf_batch_plan;
 
 int rfmf_batch_info(const rfmf_batch* b, rfmf_batch_plan* out);

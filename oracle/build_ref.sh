@@ -1,6 +1,7 @@
 #!/usr/bin/env bash
 # Build oracle/_ref/libref_host.so from the reference's own host sources, where
-# they lie, plus oracle/ref_harness.cpp.  Test infrastructure: used only to pin
+# they lie, plus oracle/ref_harness.cpp, and oracle/_ref/anneal_kernels.cubin
+# from the reference's kernel source (device code, launched by oracle/refgpu.cpp).  Test infrastructure: used only to pin
 # the oracle and to regenerate tests/golden/.  Needs the reference checkout
 # (default /root/reference, or $RFMF_REFERENCE); exits 0 without building when
 # it is absent, as on a machine that only has this repository.
@@ -18,3 +19,7 @@ g++ -std=c++17 -O2 -fPIC -shared -I"$ref/src" \
     "$ref/src/read_gset.cpp" "$ref/src/graph.cpp" \
     -o "$here/_ref/libref_host.so"
 echo "build_ref: built $here/_ref/libref_host.so"
+# The reference's kernel TU, device code only, unchanged, for sm_103a.
+nvcc -cubin -gencode arch=compute_103a,code=sm_103a -std=c++17 -O2 -I"$ref/src" \
+    "$ref/src/anneal_kernels.cu" -o "$here/_ref/anneal_kernels.cubin"
+echo "build_ref: built $here/_ref/anneal_kernels.cubin"

@@ -60,7 +60,8 @@ class BatchPlan(ct.Structure):
     _fields_ = [("nchains", ct.c_int64), ("total_sweeps", ct.c_uint64),
                 ("threads_per_chain", ct.c_int), ("chains_per_cta", ct.c_int),
                 ("grid", ct.c_int), ("items", ct.c_int), ("score64", ct.c_int),
-                ("csr_format", ct.c_int), ("gain_width", ct.c_int), ("smem_bytes", ct.c_int)]
+                ("csr_format", ct.c_int), ("gain_width", ct.c_int), ("smem_bytes", ct.c_int),
+                ("balanced", ct.c_int)]
 
 
 STATUS = {0: "RFMF_OK", 1: "RFMF_ERR_INVALID", 2: "RFMF_ERR_CUDA", 3: "RFMF_ERR_NOMEM",

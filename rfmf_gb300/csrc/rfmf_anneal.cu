@@ -296,11 +296,13 @@ struct ChainSmem {
     unsigned char* D;
     uint32_t* bits;
     uint32_t* best;
+    unsigned char* sb;           // spins as bytes (1 = +1), kept equal to bits
     unsigned long long* slots;   // int32 mode: packed keys
     long long* scores;           // int64 mode: max score per group (aliases slots)
     int32_t* ids;                // int64 mode: winner id per group
     int32_t* win;                // winners of the current sweep
     int64_t* red;                // one partial per warp of the group
+    int32_t* tk;                 // compact-key Gumbel table of this chain
 };
 
 __device__ __forceinline__ ChainSmem carve_chain(unsigned char* base, const DevLaunch& L,
@@ -310,11 +312,13 @@ __device__ __forceinline__ ChainSmem carve_chain(unsigned char* base, const DevL
     s.D = base + c.d;
     s.bits = reinterpret_cast<uint32_t*>(base + c.bits);
     s.best = reinterpret_cast<uint32_t*>(base + c.best);
+    s.sb = base + c.sb;
     s.slots = reinterpret_cast<unsigned long long*>(base + c.slots);
     s.scores = reinterpret_cast<long long*>(base + c.slots);
     s.ids = reinterpret_cast<int32_t*>(base + c.ids);
     s.win = reinterpret_cast<int32_t*>(base + c.win);
     s.red = reinterpret_cast<int64_t*>(base + c.red);
+    s.tk = reinterpret_cast<int32_t*>(base + c.tk);
     return s;
 }
 
@@ -347,38 +351,6 @@ __device__ __forceinline__ int32_t group_sum32(int32_t v, const ChainSmem& s, in
 // Scores every vertex from pre-sweep D and leaves the winner of every group
 // g < P in the chain's slots (int32 mode: packed key; int64 mode: ids[g]).
 // Slots start each sweep at their empty value (reset by FLIP's reader).
-
-struct Acc32 {
-    int32_t s[8];
-    uint32_t b[8];
-};
-
-// Branch-free running max with strict improvement: blocks arrive in
-// increasing order, so a tie keeps the earlier (smaller) vertex.
-__device__ __forceinline__ void upd32(Acc32& a, int j, int32_t sc, uint32_t b) {
-    const bool gt = sc > a.s[j];
-    a.b[j] = gt ? b : a.b[j];
-    a.s[j] = max(a.s[j], sc);
-}
-
-// int32 scores, scaled by 16: with r the 11-bit field, f = r and
-// 16*gum = 16*LUT[r & 15] + 16*(r >> 4) = T16[r & 15] + r, where
-// T16[i] = 16*LUT[i] - i.  So 16*score = (16 beta) d + T16[r & 15] + r: an
-// exact scaling (same order, same ties) that needs no separate dither field.
-// The host enables it only when 16 * (betaMax * B + max|gum|) + 2047 < 2^31.
-__device__ __forceinline__ void score8_32(Acc32& a, const uint32_t x[4], const int32_t d[8],
-                                          int32_t beta16, const int32_t* t16, uint32_t b,
-                                          int lim) {
-#pragma unroll
-    for (int w = 0; w < 4; ++w) {
-        const uint32_t f0 = x[w] & 0x7FFu;
-        const uint32_t f1 = (x[w] >> 16) & 0x7FFu;
-        if (2 * w < lim)
-            upd32(a, 2 * w, beta16 * d[2 * w] + t16[f0 & 15u] + static_cast<int32_t>(f0), b);
-        if (2 * w + 1 < lim)
-            upd32(a, 2 * w + 1, beta16 * d[2 * w + 1] + t16[f1 & 15u] + static_cast<int32_t>(f1), b);
-    }
-}
 
 // Per-phase constants, recomputed only when P changes (no integer division
 // or modulo by P inside a sweep).
@@ -415,74 +387,124 @@ __device__ __forceinline__ unsigned long long warp_max_key(unsigned long long k)
     return (static_cast<unsigned long long>(mhi) << 32) | mlo;
 }
 
+// Compact int32 argmax key.  A thread visits its vertex blocks b = t + k*T
+// for k = 0, 1, ... (at most 2^kb of them); lane j of block k gets
+//   key = score * 2^kb + (2^kb - 1 - k),   score = gum + beta * delta,
+// so one integer max per vertex keeps the best score and, among equal
+// scores, the smallest k, i.e. the smallest vertex (v = 8(t + kT) + j grows
+// with k).  With f the 11-bit field and i = f & 15,
+//   gum * 2^kb = LUT[i] * 2^kb + (f >> 4) * 2^kb
+//              = (LUT[i] * 2^kb - i * 2^(kb-4)) + f * 2^(kb-4)     (kb >= 4)
+// so key = TK[i] + f * 2^(kb-4) + (beta * 2^kb) * delta + (2^kb - 1 - k) with a
+// per-chain 16-entry table TK.  The host enables this path only when
+// (betaMax * B + max|gum| + 1) * 2^kb < 2^31 for every chain, so every key and
+// partial sum is exact in int32; otherwise the launch takes the int64 path.
+struct KeyCfg {
+    int kb;          // bits of the block-iteration field
+    int fshift;      // kb - 4
+};
+
+__device__ __forceinline__ int key_bits(int n, int T) {
+    const int iters = ((n + 7) / 8 + T - 1) / T;
+    int kb = 4;
+    while ((1 << kb) < iters) ++kb;
+    return kb;
+}
+
+__device__ __forceinline__ void score8_key(int32_t acc[8], const uint32_t x[4], const int32_t d[8],
+                                           int32_t betaK, int32_t ck, int fshift,
+                                           const int32_t* tk, int lim) {
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        const uint32_t f0 = x[w] & 0x7FFu;
+        const uint32_t f1 = (x[w] >> 16) & 0x7FFu;
+        if (2 * w < lim) {
+            const int32_t k0 = tk[f0 & 15u] + static_cast<int32_t>(f0 << fshift) +
+                               betaK * d[2 * w] + ck;
+            acc[2 * w] = max(acc[2 * w], k0);
+        }
+        if (2 * w + 1 < lim) {
+            const int32_t k1 = tk[f1 & 15u] + static_cast<int32_t>(f1 << fshift) +
+                               betaK * d[2 * w + 1] + ck;
+            acc[2 * w + 1] = max(acc[2 * w + 1], k1);
+        }
+    }
+}
+
 template <class DP>
-__device__ void select32(const ChainSmem& s, const int32_t* t16, int n, const PhaseCfg& pc,
-                         int32_t beta, uint64_t step, const ChainKeys& keys, int t, int T) {
+__device__ void select32(const ChainSmem& s, const int32_t* lut, const int32_t* tk,
+                         const KeyCfg& kc, int n, const PhaseCfg& pc, int32_t beta,
+                         uint64_t step, const ChainKeys& keys, int t, int T) {
     const SweepConst sc = make_sweep(step, keys);
-    const int32_t beta16 = beta * 16;
     const int nfull = n >> 3;
     const int P = pc.P;
+    const int M = (1 << kc.kb) - 1;
     if (pc.mode != 2) {
-        Acc32 a;
+        const int32_t betaK = beta * (1 << kc.kb);
+        int32_t acc[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) { a.s[j] = INT32_MIN; a.b[j] = 0; }
-        int b = t;
-        for (; b + T < nfull; b += 2 * T) {
+        for (int j = 0; j < 8; ++j) acc[j] = INT32_MIN;
+        int b = t, k = 0;
+        for (; b + T < nfull; b += 2 * T, k += 2) {
             uint32_t xa[4], xb[4];
             int32_t da[8], db[8];
             philox_block(static_cast<uint32_t>(b), sc, keys, xa);
             philox_block(static_cast<uint32_t>(b + T), sc, keys, xb);
             DP::load8(s.D, b, da);
             DP::load8(s.D, b + T, db);
-            score8_32(a, xa, da, beta16, t16, static_cast<uint32_t>(b), 8);
-            score8_32(a, xb, db, beta16, t16, static_cast<uint32_t>(b + T), 8);
+            score8_key(acc, xa, da, betaK, M - k, kc.fshift, tk, 8);
+            score8_key(acc, xb, db, betaK, M - k - 1, kc.fshift, tk, 8);
         }
         if (b < nfull) {
             uint32_t xa[4];
             int32_t da[8];
             philox_block(static_cast<uint32_t>(b), sc, keys, xa);
             DP::load8(s.D, b, da);
-            score8_32(a, xa, da, beta16, t16, static_cast<uint32_t>(b), 8);
+            score8_key(acc, xa, da, betaK, M - k, kc.fshift, tk, 8);
             b += T;
+            ++k;
         }
         if ((n & 7) && b == nfull) {
             uint32_t xa[4];
             int32_t da[8];
             philox_block(static_cast<uint32_t>(b), sc, keys, xa);
             DP::load8(s.D, b, da);
-            score8_32(a, xa, da, beta16, t16, static_cast<uint32_t>(b), n & 7);
+            score8_key(acc, xa, da, betaK, M - k, kc.fshift, tk, n & 7);
         }
-        unsigned long long k[8];
+        // Back to (score, v) as a packed 64-bit key for the group reduction.
+        unsigned long long key[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-            k[j] = (a.s[j] == INT32_MIN) ? 0ull
-                                         : pack_key(a.s[j], static_cast<int32_t>(8 * a.b[j] + j));
+        for (int j = 0; j < 8; ++j) {
+            const int kk = M - (acc[j] & M);
+            const int v = 8 * (t + kk * T) + j;
+            key[j] = (acc[j] == INT32_MIN) ? 0ull : pack_key(acc[j] >> kc.kb, v);
+        }
         if (pc.mode == 0) {
             // Groups repeat every P/8 lanes inside a warp's 256 vertices:
             // fold accumulators (P < 8) and lanes that share a group.
             if (P <= 4) {
 #pragma unroll
-                for (int j = 0; j < 4; ++j) if (k[j + 4] > k[j]) k[j] = k[j + 4];
+                for (int j = 0; j < 4; ++j) if (key[j + 4] > key[j]) key[j] = key[j + 4];
             }
             if (P <= 2) {
 #pragma unroll
-                for (int j = 0; j < 2; ++j) if (k[j + 2] > k[j]) k[j] = k[j + 2];
+                for (int j = 0; j < 2; ++j) if (key[j + 2] > key[j]) key[j] = key[j + 2];
             }
             if (P == 1) {
-                if (k[1] > k[0]) k[0] = k[1];
+                if (key[1] > key[0]) key[0] = key[1];
             }
             if (P <= 8) {
 #pragma unroll
                 for (int j = 0; j < 8; ++j)
-                    if (j < pc.jn) k[j] = warp_max_key(k[j]);
+                    if (j < pc.jn) key[j] = warp_max_key(key[j]);
             } else {
 #pragma unroll
                 for (int m = 16; m >= 2; m >>= 1) {
                     if (m >= pc.period) {
 #pragma unroll
                         for (int j = 0; j < 8; ++j) {
-                            const unsigned long long o = shfl_xor_u64(k[j], m);
-                            if (o > k[j]) k[j] = o;
+                            const unsigned long long o = shfl_xor_u64(key[j], m);
+                            if (o > key[j]) key[j] = o;
                         }
                     }
                 }
@@ -492,10 +514,10 @@ __device__ void select32(const ChainSmem& s, const int32_t* t16, int n, const Ph
                 // lane < P/8 (or lane 0): group 8*lane + j (or j) is < P.
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
-                    if (j < pc.jn && k[j]) {
+                    if (j < pc.jn && key[j]) {
                         const int g = 8 * lane + j;
-                        if (T == 32) s.slots[g] = k[j];
-                        else atomicMax(&s.slots[g], k[j]);
+                        if (T == 32) s.slots[g] = key[j];
+                        else atomicMax(&s.slots[g], key[j]);
                     }
                 }
             }
@@ -503,24 +525,24 @@ __device__ void select32(const ChainSmem& s, const int32_t* t16, int n, const Ph
             int g = pc.g0;
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                if (k[j]) atomicMax(&s.slots[g], k[j]);
+                if (key[j]) atomicMax(&s.slots[g], key[j]);
                 if (++g == P) g = 0;
             }
         }
     } else {
-        // General P: one shared atomic per vertex.
-        for (int b = t; 8 * b < n; b += T) {
+        // General P: one shared atomic per vertex, plain score.
+        for (int bb = t; 8 * bb < n; bb += T) {
             uint32_t x[4];
             int32_t d[8];
-            philox_block(static_cast<uint32_t>(b), sc, keys, x);
-            DP::load8(s.D, b, d);
-            int g = (8 * b) % P;
+            philox_block(static_cast<uint32_t>(bb), sc, keys, x);
+            DP::load8(s.D, bb, d);
+            int g = (8 * bb) % P;
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                const int v = 8 * b + j;
+                const int v = 8 * bb + j;
                 if (v < n) {
                     const uint32_t r = field(x, j);
-                    const int32_t sv = beta16 * d[j] + t16[r & 15u] + static_cast<int32_t>(r);
+                    const int32_t sv = lut[r & 15u] + static_cast<int32_t>(r >> 4) + beta * d[j];
                     atomicMax(&s.slots[g], pack_key(sv, v));
                 }
                 if (++g == P) g = 0;
@@ -609,7 +631,7 @@ __device__ void select64(const ChainSmem& s, const int32_t* lut, int n, const Ph
 // ------------------------------------------------------------------ chain
 template <class DP, int kFmt, bool kS64>
 __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView& csr,
-                          const int32_t* lut, const int32_t* t16, int ci, int t, int T, int grp) {
+                          const int32_t* lut, int ci, int t, int T, int grp) {
     DevChain& ch = L.chains[ci];
     if (ch.sweepsDone >= ch.sweepsTotal && ch.cur != kUnsetCut) return;
     const DevGraph& g = L.graphs[ch.graph];
@@ -628,10 +650,17 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
         s.slots[i] = kS64 ? static_cast<unsigned long long>(LLONG_MIN) : 0ull;
         s.ids[i] = INT32_MAX;
     }
+    KeyCfg kc;
+    kc.kb = key_bits(n, T);
+    kc.fshift = kc.kb - 4;
+    if (t < 16) s.tk[t] = lut[t] * (1 << kc.kb) - t * (1 << kc.fshift);
+    group_sync(grp, T);
+    const int nPad = (n + 7) & ~7;
+    for (int v = t; v < nPad; v += T)
+        s.sb[v] = (v < n) ? static_cast<unsigned char>(spin_of(s.bits, v)) : 0;
     group_sync(grp, T);
 
     // ---- D[v] = spin[v] * sum_u w(v,u) spin[u]; padding past n is 0
-    const int nPad = (n + 7) & ~7;
     int64_t dsum = 0;
     for (int v = t; v < nPad; v += T) {
         int32_t d = 0;
@@ -642,9 +671,9 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
             for (uint32_t i = lo; i < hi; ++i) {
                 int col, w;
                 Csr<kFmt>::entry(csr, i, col, w);
-                acc += spin_of(s.bits, col) ? w : -w;
+                acc += s.sb[col] ? w : -w;
             }
-            d = spin_of(s.bits, v) ? acc : -acc;
+            d = s.sb[v] ? acc : -acc;
             dsum += d;
         }
         DP::set(s.D, v, d);
@@ -717,7 +746,7 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
         const uint64_t step = sw + 1;   // 1-based sweep id
 
         if constexpr (kS64) select64<DP>(s, lut, n, pc, beta, step, keys, t, T, grp);
-        else select32<DP>(s, t16, n, pc, beta, step, keys, t, T);
+        else select32<DP>(s, lut, s.tk, kc, n, pc, beta, step, keys, t, T);
         group_sync(grp, T);
 
         // ---- FLIP 1: winners; negate their gains, flip their spins
@@ -741,6 +770,7 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
                 loc += d;
                 DP::set(s.D, v, -d);
                 atomicXor(&s.bits[v >> 5], 1u << (v & 31));
+                s.sb[v] ^= 1u;
             }
         }
         group_sync(grp, T);
@@ -753,7 +783,7 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
             for (int gi = t >> pc.laneShift; gi < P; gi += T >> pc.laneShift) {
                 const int v = s.win[gi];
                 if (v < 0) continue;
-                const int sv = spin_of(s.bits, v);
+                const int sv = s.sb[v];
                 uint32_t lo, hi;
                 Csr<kFmt>::row(csr, v, lo, hi);
                 uint32_t i = lo + sub;
@@ -763,8 +793,8 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
                     Csr<kFmt>::entry(csr, i + lanes, c1, w1);
                     Csr<kFmt>::entry(csr, i + 2 * lanes, c2, w2);
                     Csr<kFmt>::entry(csr, i + 3 * lanes, c3, w3);
-                    const int s0b = spin_of(s.bits, c0), s1b = spin_of(s.bits, c1);
-                    const int s2b = spin_of(s.bits, c2), s3b = spin_of(s.bits, c3);
+                    const int s0b = s.sb[c0], s1b = s.sb[c1];
+                    const int s2b = s.sb[c2], s3b = s.sb[c3];
                     DP::add(s.D, c0, (sv == s0b) ? 2 * w0 : -2 * w0);
                     DP::add(s.D, c1, (sv == s1b) ? 2 * w1 : -2 * w1);
                     DP::add(s.D, c2, (sv == s2b) ? 2 * w2 : -2 * w2);
@@ -773,7 +803,7 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
                 for (; i < hi; i += lanes) {
                     int c0, w0;
                     Csr<kFmt>::entry(csr, i, c0, w0);
-                    DP::add(s.D, c0, (sv == spin_of(s.bits, c0)) ? 2 * w0 : -2 * w0);
+                    DP::add(s.D, c0, (sv == s.sb[c0]) ? 2 * w0 : -2 * w0);
                 }
             }
         }
@@ -876,7 +906,6 @@ __global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) 
     using DP = typename std::conditional<kDBytes == 1, D8, D32>::type;
     extern __shared__ __align__(128) unsigned char smem[];
     int32_t* lut = reinterpret_cast<int32_t*>(smem);                 // 64 B
-    int32_t* t16 = reinterpret_cast<int32_t*>(smem + 64);            // 64 B
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + 128);        // 8 B
     int* sItem = reinterpret_cast<int*>(smem + 144);
     unsigned char* csrBase = smem + kSmemHeader;
@@ -887,10 +916,7 @@ __global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) 
     const int t = threadIdx.x - grp * T;
     const ChainSmem cs = carve_chain(chainBase + static_cast<size_t>(grp) * L.chainBytes, L, kDBytes);
 
-    if (threadIdx.x < 16) {
-        lut[threadIdx.x] = L.lut[threadIdx.x];
-        t16[threadIdx.x] = 16 * L.lut[threadIdx.x] - static_cast<int32_t>(threadIdx.x);
-    }
+    if (threadIdx.x < 16) lut[threadIdx.x] = L.lut[threadIdx.x];
     if (kFmt != kCsrGlobal && threadIdx.x == 0) mbar_init(mbar);
     __syncthreads();
 
@@ -908,6 +934,8 @@ __global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) 
             __syncthreads();
             continue;
         }
+        uint64_t t0 = 0;
+        if (threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
         const DevGraph& g = L.graphs[item.graph];
         CsrView csr;
         if constexpr (kFmt == kCsrGlobal) {
@@ -928,8 +956,13 @@ __global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) 
         }
         __syncthreads();
         if (!dead && grp < item.count && grp < L.chainsPerCta)
-            run_chain<DP, kFmt, kS64>(L, cs, csr, lut, t16, L.order[item.first + grp], t, T, grp);
+            run_chain<DP, kFmt, kS64>(L, cs, csr, lut, L.order[item.first + grp], t, T, grp);
         __syncthreads();
+        if (threadIdx.x == 0 && L.itemNs) {
+            uint64_t t1;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+            L.itemNs[it] = t1 - t0;
+        }
     }
 }
 

@@ -106,6 +106,7 @@ struct DevLaunch {
     int32_t*           queue;       // work-queue head (zeroed before the launch)
     int32_t*           error;       // first device error (DevError)
     int32_t*           errorItem;   // chain/item that raised it
+    uint64_t*          itemNs;      // per item: device time the CTA spent on it (ns)
     uint64_t           window;      // sweeps each chain advances in this launch
     int32_t            lut[16];     // Q20 Gumbel quantile table
 };
@@ -115,7 +116,7 @@ struct DevLaunch {
 constexpr int64_t kUnsetCut = INT64_MIN;
 
 // Shared-memory header in front of the CSR region: Gumbel table (64 B),
-// scaled Gumbel table (64 B), bulk-copy mbarrier, work-item slot.
+// bulk-copy mbarrier, work-item slot.
 constexpr uint32_t kSmemHeader = 256;
 
 #if defined(__CUDACC__)
@@ -127,10 +128,12 @@ constexpr uint32_t kSmemHeader = 256;
 RFMF_HD uint32_t align16(uint32_t x) { return (x + 15u) & ~15u; }
 
 // Per-chain shared-memory region, in order: gains D (nPad * dbytes), spin
-// bits, best-spin bits, group key slots (8 B), ids (4 B), winners (4 B),
-// reduction partials (8 B per warp).  Host and kernel both carve with this.
+// bits, best-spin bits, spins as bytes (0/1, for one-load neighbour lookups
+// in FLIP), group key slots (8 B), ids (4 B), winners (4 B),
+// reduction partials (8 B per warp), compact-key Gumbel table (16 x 4 B).
+// Host and kernel both carve with this.
 struct ChainLayout {
-    uint32_t d, bits, best, slots, ids, win, red, total;
+    uint32_t d, bits, best, sb, slots, ids, win, red, tk, total;
 };
 
 RFMF_HD ChainLayout chain_layout(int maxN, int maxWords, int pmax, int warps, int dbytes) {
@@ -140,10 +143,12 @@ RFMF_HD ChainLayout chain_layout(int maxN, int maxWords, int pmax, int warps, in
     c.d = o;     o = align16(o + nPad * static_cast<uint32_t>(dbytes));
     c.bits = o;  o = align16(o + static_cast<uint32_t>(maxWords) * 4u);
     c.best = o;  o = align16(o + static_cast<uint32_t>(maxWords) * 4u);
+    c.sb = o;    o = align16(o + nPad);
     c.slots = o; o = align16(o + static_cast<uint32_t>(pmax) * 8u);
     c.ids = o;   o = align16(o + static_cast<uint32_t>(pmax) * 4u);
     c.win = o;   o = align16(o + static_cast<uint32_t>(pmax) * 4u);
     c.red = o;   o = align16(o + static_cast<uint32_t>(warps) * 8u);
+    c.tk = o;    o = align16(o + 16u * 4u);
     c.total = o;
     return c;
 }

@@ -190,15 +190,6 @@ bool score_safe_int32(int64_t total, double t0, int64_t B) {
     return (bmf * B + kGumbelMaxMag) < static_cast<int64_t>(std::numeric_limits<int32_t>::max());
 }
 
-// The kernel's int32 path: 16 * (betaMax * B + max|gum|) + 2047 < 2^31,
-// with betaMax = beta_fixed(total) (beta is monotone in the step).
-bool score_safe_int32_scaled(int64_t total, double t0, int64_t B) {
-    const double bmax = std::round(std::log(1.0 + static_cast<double>(std::max<int64_t>(total, 1))) /
-                                   t0 * 1048576.0);
-    return 16.0 * (bmax * static_cast<double>(B) + static_cast<double>(kGumbelMaxMag)) + 2047.0 <
-           2147483647.0;
-}
-
 // Owning device buffer.
 struct DevBuf {
     void* p = nullptr;
@@ -236,6 +227,10 @@ struct rfmf_graph {
     bool unit16 = false, packed32 = false;
     uint32_t offBytes = 0, u16Bytes = 0, p32Bytes = 0;
     DevBuf offsets, edges, u16, p32;
+    // Learned cost: device ns per chain-sweep of one CTA slot, from the item
+    // timings of earlier launches (weight = chain-sweeps observed).  Feeds the
+    // work-item sizing of later launches; never affects results.
+    mutable double costNs = 0.0, costWeight = 0.0;
 };
 
 struct rfmf_batch {
@@ -250,8 +245,18 @@ struct rfmf_batch {
     std::vector<int64_t> graphOfChain;
     int64_t words = 0;                           // total spin words over chains
     DevBuf dGraphs, dScheds, dChains, dItems, dOrder, dPhaseP, dPhaseIters, dBetaEnd, dBetaVal,
-        dBits, dBest, dCtl;
+        dBits, dBest, dCtl, dItemNs;
     DevLaunch L{};
+    // Work-item state: graphs, their chains, current per-graph chains per item.
+    std::vector<const rfmf_graph*> glist;
+    std::vector<std::vector<int32_t>> chainsOf;
+    std::vector<int> Kg;
+    std::vector<DevItem> items;
+    std::vector<int32_t> order;
+    int occ = 1;                 // resident CTAs per SM for the launch shape
+    bool balanced = false;       // items sized from learned graph costs
+    uint64_t hostDone = 0;       // sweeps every chain has been advanced by
+    uint64_t pendingSweeps = 0;  // sweeps of launches whose item times are unread
     cudaGraphExec_t graphExec = nullptr;
     uint64_t graphSweeps = 0;
     int graphLaunches = 0;
@@ -521,8 +526,36 @@ namespace {
 //  * K: the smallest number of chains per CTA that lets every work item be
 //    resident at once (one wave), within shared memory, 512 threads per CTA
 //    and the named-barrier budget; with more chains than that, the largest.
+// Warps per chain: one unless a chain has enough vertex blocks to keep more
+// warps busy (about 384 blocks of 8 vertices per extra warp).
+int choose_warps(int maxN, const rfmf_launch_config& c) {
+    if (c.threads_per_chain) return c.threads_per_chain / 32;
+    int W = 1;
+    const int nblk = (maxN + 7) / 8;
+    while (W < 4 && nblk >= 384 * 2 * W) W *= 2;
+    return W;
+}
+
+// Bits of the block-iteration field of the compact int32 key (kernel
+// key_bits): ceil(log2(blocks per thread)), at least 4.
+int key_bits(int64_t n, int T) {
+    const int64_t iters = ((n + 7) / 8 + T - 1) / T;
+    int kb = 4;
+    while ((int64_t(1) << kb) < iters) ++kb;
+    return kb;
+}
+
+// The kernel's int32 path packs score * 2^kb + (2^kb - 1 - k) into one int:
+// (betaMax * B + max|gum| + 1) * 2^kb must stay below 2^31.
+bool compact_key_safe(int64_t total, double t0, int64_t B, int kb) {
+    const double bmax = std::round(std::log(1.0 + static_cast<double>(std::max<int64_t>(total, 1))) /
+                                   t0 * 1048576.0);
+    return (bmax * static_cast<double>(B) + static_cast<double>(kGumbelMaxMag) + 1.0) *
+               std::ldexp(1.0, kb) < 2147483647.0;
+}
+
 struct Plan {
-    int dbytes, fmt, warps, K, threads, grid, nitems, pmax;
+    int dbytes, fmt, warps, K, Kuniform, threads, grid, nitems, pmax, occ;
     uint32_t csrBytes, chainBytes;
     size_t smem;
 };
@@ -547,15 +580,7 @@ int plan_launch(rfmf_batch& b, const std::vector<const rfmf_graph*>& glist,
     else if (c.csr_format == 3) fmt = kCsrGlobal;
     else return fail(RFMF_ERR_INVALID, "csr_format must be 0..3");
     // warps per chain
-    int W = 1;
-    if (c.threads_per_chain) {
-        if (c.threads_per_chain != 32 && c.threads_per_chain != 64 && c.threads_per_chain != 128)
-            return fail(RFMF_ERR_INVALID, "threads_per_chain must be 0, 32, 64 or 128");
-        W = c.threads_per_chain / 32;
-    } else {
-        const int nblk = (maxN + 7) / 8;
-        while (W < 4 && nblk >= 384 * 2 * W) W *= 2;
-    }
+    const int W = choose_warps(maxN, c);
     const void* kern = kernel_ptr(pl.dbytes, kCsrGlobal, b.score64);
     cudaFuncAttributes fa{};
     CU(cudaFuncGetAttributes(&fa, kern));
@@ -589,34 +614,126 @@ int plan_launch(rfmf_batch& b, const std::vector<const rfmf_graph*>& glist,
             for (int64_t cg : perGraphChains) it += (cg + K - 1) / K;
             return it;
         };
-        int bestK = Kmax, bestOcc = 0;
-        for (int K = c.chains_per_cta ? Kmax : 1; K <= Kmax; ++K) {
-            const size_t smem = kSmemHeader + csrBytes + static_cast<size_t>(K) * chainBytes;
-            int occ = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k2, 32 * W * K, smem) != cudaSuccess) {
+        // CTA shape: Kmax warp groups (headroom for uneven per-graph items);
+        // the first launch uses the smallest uniform K that fits one wave.
+        int occ = 0;
+        int Kshape = Kmax;
+        for (; Kshape >= 1; --Kshape) {
+            const size_t smem = kSmemHeader + csrBytes + static_cast<size_t>(Kshape) * chainBytes;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k2, 32 * W * Kshape, smem) !=
+                cudaSuccess) {
                 cudaGetLastError();
                 occ = 0;
             }
-            if (occ <= 0) continue;
-            bestK = K;
-            bestOcc = occ;
-            if (items_for(K) <= static_cast<int64_t>(occ) * sms) break;
+            if (occ > 0) break;
         }
-        if (bestOcc <= 0)
+        if (Kshape < 1 || occ <= 0)
             return fail(RFMF_ERR_CAPACITY, "no resident configuration for %u B CSR + %u B per chain",
                         csrBytes, chainBytes);
+        const int64_t slots = static_cast<int64_t>(occ) * sms;
+        int Kuni = c.chains_per_cta ? Kshape : 1;
+        while (Kuni < Kshape && items_for(Kuni) > slots) ++Kuni;
+        pl.occ = occ;
         pl.fmt = fmt;
         pl.warps = W;
-        pl.K = bestK;
-        pl.threads = 32 * W * bestK;
+        pl.K = Kshape;
+        pl.Kuniform = Kuni;
+        pl.threads = 32 * W * Kshape;
         pl.csrBytes = csrBytes;
         pl.chainBytes = chainBytes;
-        pl.smem = kSmemHeader + csrBytes + static_cast<size_t>(bestK) * chainBytes;
-        pl.nitems = static_cast<int>(items_for(bestK));
-        pl.grid = static_cast<int>(std::min<int64_t>(pl.nitems, static_cast<int64_t>(bestOcc) * sms));
+        pl.smem = kSmemHeader + csrBytes + static_cast<size_t>(Kshape) * chainBytes;
+        pl.nitems = static_cast<int>(items_for(Kuni));
+        pl.grid = static_cast<int>(std::min<int64_t>(pl.nitems, slots));
         return RFMF_OK;
     }
     return fail(RFMF_ERR_CAPACITY, "no launch plan");
+}
+
+}  // namespace
+
+namespace {
+
+// Per-graph chains per item.  With learned costs c_g (ns per chain-sweep of a
+// CTA slot) for every graph, pick the smallest per-sweep makespan tau such
+// that items of K_g = min(K, floor(tau / c_g)) chains all fit the resident
+// CTA slots; without costs every graph uses the planned K.
+void plan_balanced(rfmf_batch& b) {
+    const size_t G = b.glist.size();
+    bool known = true;
+    for (const rfmf_graph* g : b.glist) known = known && g->costNs > 0.0;
+    if (!known || G < 2) { b.balanced = false; return; }
+    const int64_t slots = static_cast<int64_t>(b.occ) * b.ctx->sms;
+    double lo = 0.0, hi = 0.0;
+    for (const rfmf_graph* g : b.glist) hi = std::max(hi, g->costNs * b.K);
+    auto fits = [&](double tau, std::vector<int>& kg) {
+        int64_t items = 0;
+        for (size_t k = 0; k < G; ++k) {
+            int q = static_cast<int>(std::floor(tau / b.glist[k]->costNs));
+            q = std::max(1, std::min(b.K, q));
+            kg[k] = q;
+            items += (static_cast<int64_t>(b.chainsOf[k].size()) + q - 1) / q;
+        }
+        return items <= slots;
+    };
+    std::vector<int> kg(G, b.K), best(G, b.K);
+    if (!fits(hi, kg)) { b.balanced = false; return; }
+    best = kg;
+    for (int it = 0; it < 60; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (fits(mid, kg)) { hi = mid; best = kg; } else { lo = mid; }
+    }
+    b.Kg = best;
+    b.balanced = true;
+}
+
+// Items: graphs in decreasing per-item cost, each graph's chains in groups of
+// its K_g.  Rewrites the host copies; the caller uploads them.
+void build_items(rfmf_batch& b) {
+    const size_t G = b.glist.size();
+    std::vector<int> gorder(G);
+    for (size_t k = 0; k < G; ++k) gorder[k] = static_cast<int>(k);
+    auto itemCost = [&](int k) {
+        const double c = b.glist[k]->costNs > 0.0 ? b.glist[k]->costNs
+                                                    : static_cast<double>(b.glist[k]->n);
+        return c * b.Kg[k];
+    };
+    std::stable_sort(gorder.begin(), gorder.end(), [&](int a, int z) { return itemCost(a) > itemCost(z); });
+    b.items.clear();
+    b.order.clear();
+    for (int gk : gorder) {
+        const auto& cl = b.chainsOf[gk];
+        const size_t K = static_cast<size_t>(b.Kg[gk]);
+        for (size_t s = 0; s < cl.size(); s += K) {
+            DevItem it{};
+            it.graph = gk;
+            it.first = static_cast<int32_t>(b.order.size());
+            it.count = static_cast<int32_t>(std::min(K, cl.size() - s));
+            for (int q = 0; q < it.count; ++q) b.order.push_back(cl[s + q]);
+            b.items.push_back(it);
+        }
+    }
+    b.nitems = static_cast<int>(b.items.size());
+    b.grid = static_cast<int>(std::min<int64_t>(b.nitems, static_cast<int64_t>(b.occ) * b.ctx->sms));
+    b.L.nitems = b.nitems;
+}
+
+// Fold the item timings of completed launches into the graphs' costs.
+int harvest_item_times(rfmf_batch& b) {
+    if (!b.pendingSweeps || b.items.empty()) return RFMF_OK;
+    const uint64_t sweeps = b.pendingSweeps;
+    b.pendingSweeps = 0;
+    std::vector<uint64_t> ns(b.items.size());
+    CU(cudaMemcpy(ns.data(), b.dItemNs.p, ns.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < b.items.size(); ++i) {
+        const DevItem& it = b.items[i];
+        if (ns[i] == 0 || it.count <= 0) continue;
+        const double w = static_cast<double>(it.count) * static_cast<double>(sweeps);
+        const double c = static_cast<double>(ns[i]) / w;
+        const rfmf_graph* g = b.glist[it.graph];
+        g->costNs = (g->costNs * g->costWeight + c * w) / (g->costWeight + w);
+        g->costWeight += w;
+    }
+    return RFMF_OK;
 }
 
 }  // namespace
@@ -675,16 +792,22 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
         maxB = std::max(maxB, g->B);
     }
 
-    // Score path.  The int32 kernel path scores 16 * (gum + beta * delta)
-    // (exact, see score8_32), so it needs the reference's gate
-    // (src/host_common.cpp:296-312) with 16x headroom at every chain's
-    // (t0, B); otherwise the launch takes the exact int64 path.  Either way
-    // the winners are the reference's.
+    // Score path.  The int32 kernel path packs each score with its block
+    // iteration into one int (compact key, see select32), so it needs
+    // (betaMax * B + max|gum| + 1) * 2^kb < 2^31 at every chain's (t0, B, n);
+    // otherwise the launch takes the exact int64 path (the reference's
+    // int64 two-pass route, src/anneal_kernels.cu:348-378).  Either way the
+    // winners are the reference's.
+    if (c.threads_per_chain && c.threads_per_chain != 32 && c.threads_per_chain != 64 &&
+        c.threads_per_chain != 128)
+        return fail(RFMF_ERR_INVALID, "threads_per_chain must be 0, 32, 64 or 128");
     b->score64 = false;
     if (c.score_path == 2) b->score64 = true;
     else {
+        const int T = 32 * choose_warps(maxN, c);
         for (int64_t i = 0; i < C && !b->score64; ++i)
-            if (!score_safe_int32_scaled(static_cast<int64_t>(total), t0s[i], graphs[i]->B))
+            if (!compact_key_safe(static_cast<int64_t>(total), t0s[i], graphs[i]->B,
+                                  key_bits(graphs[i]->n, T)))
                 b->score64 = true;
         if (b->score64 && c.score_path == 1)
             return fail(RFMF_ERR_INVALID, "int32 scores would overflow for this (t0, B, sweeps)");
@@ -708,7 +831,6 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
     b->K = pl.K;
     b->threads = pl.threads;
     b->grid = pl.grid;
-    b->nitems = pl.nitems;
     b->smem = pl.smem;
 
     std::vector<DevGraph> hg(glist.size());
@@ -724,26 +846,15 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
         hg[k].entBytes = (pl.fmt == kCsrUnit16) ? g->u16Bytes : (pl.fmt == kCsrPacked32 ? g->p32Bytes : 0);
     }
 
-    // Work items: graphs largest first, each graph's chains in groups of K.
-    std::vector<int> gorder(glist.size());
-    for (size_t k = 0; k < gorder.size(); ++k) gorder[k] = static_cast<int>(k);
-    std::stable_sort(gorder.begin(), gorder.end(), [&](int a, int z) { return glist[a]->n > glist[z]->n; });
-    std::vector<std::vector<int32_t>> chainsOf(glist.size());
-    for (int64_t i = 0; i < C; ++i) chainsOf[b->graphOfChain[i]].push_back(static_cast<int32_t>(i));
-    std::vector<int32_t> order;
-    std::vector<DevItem> items;
-    order.reserve(C);
-    for (int gk : gorder) {
-        const auto& cl = chainsOf[gk];
-        for (size_t s = 0; s < cl.size(); s += pl.K) {
-            DevItem it{};
-            it.graph = gk;
-            it.first = static_cast<int32_t>(order.size());
-            it.count = static_cast<int32_t>(std::min<size_t>(pl.K, cl.size() - s));
-            for (int q = 0; q < it.count; ++q) order.push_back(cl[s + q]);
-            items.push_back(it);
-        }
-    }
+    // Work items: each graph's chains in groups of K (or of the per-graph
+    // sizes learned from earlier launches, see rebalance()).
+    b->glist = glist;
+    b->occ = pl.occ;
+    b->chainsOf.assign(glist.size(), {});
+    for (int64_t i = 0; i < C; ++i) b->chainsOf[b->graphOfChain[i]].push_back(static_cast<int32_t>(i));
+    b->Kg.assign(glist.size(), pl.Kuniform);
+    plan_balanced(*b);
+    build_items(*b);
 
     // Per-chain spin words and initial state.
     b->chainN.resize(C);
@@ -768,7 +879,8 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
     if ((rc = b->dGraphs.alloc(hg.size() * sizeof(DevGraph)))) return rc;
     if ((rc = b->dScheds.alloc(sizeof(DevSchedule)))) return rc;
     if ((rc = b->dChains.alloc(C * sizeof(DevChain)))) return rc;
-    if ((rc = b->dItems.alloc(items.size() * sizeof(DevItem)))) return rc;
+    if ((rc = b->dItems.alloc(C * sizeof(DevItem)))) return rc;
+    if ((rc = b->dItemNs.alloc(C * sizeof(uint64_t)))) return rc;
     if ((rc = b->dOrder.alloc(C * sizeof(int32_t)))) return rc;
     if ((rc = b->dPhaseP.alloc(std::max<int64_t>(nphases, 1) * sizeof(uint32_t)))) return rc;
     if ((rc = b->dPhaseIters.alloc(std::max<int64_t>(nphases, 1) * sizeof(uint64_t)))) return rc;
@@ -805,8 +917,8 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
     CU(cudaMemcpyAsync(b->dGraphs.p, hg.data(), hg.size() * sizeof(DevGraph), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dScheds.p, &hs, sizeof hs, cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dChains.p, hc.data(), C * sizeof(DevChain), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(b->dItems.p, items.data(), items.size() * sizeof(DevItem), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(b->dOrder.p, order.data(), C * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(b->dItems.p, b->items.data(), b->items.size() * sizeof(DevItem), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(b->dOrder.p, b->order.data(), C * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dPhaseP.p, hp.data(), hp.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dPhaseIters.p, hi.data(), hi.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dBetaEnd.p, bt.end.data(), bt.end.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
@@ -822,7 +934,8 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
     L.chains = b->dChains.as<DevChain>();
     L.items = b->dItems.as<DevItem>();
     L.order = b->dOrder.as<int32_t>();
-    L.nitems = static_cast<int32_t>(items.size());
+    L.nitems = static_cast<int32_t>(b->items.size());
+    L.itemNs = b->dItemNs.as<uint64_t>();
     L.ngraphs = static_cast<int32_t>(hg.size());
     L.nscheds = 1;
     L.warpsPerChain = pl.warps;
@@ -842,9 +955,26 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
 }
 
 namespace {
-int enqueue_run(rfmf_batch* b, uint64_t sweeps) {
+int enqueue_run(rfmf_batch* b, uint64_t sweeps, bool capturing = false) {
+    if (!capturing && !b->balanced) {
+        plan_balanced(*b);
+        if (b->balanced) {
+            build_items(*b);
+            // Stream-ordered after any launch still reading the old items.
+            CU(cudaMemcpyAsync(b->dItems.p, b->items.data(), b->items.size() * sizeof(DevItem),
+                               cudaMemcpyHostToDevice, b->ctx->stream));
+            CU(cudaMemcpyAsync(b->dOrder.p, b->order.data(), b->order.size() * sizeof(int32_t),
+                               cudaMemcpyHostToDevice, b->ctx->stream));
+            CU(cudaMemsetAsync(b->dItemNs.p, 0, b->items.size() * sizeof(uint64_t), b->ctx->stream));
+        }
+    }
     DevLaunch L = b->L;
     L.window = sweeps;
+    if (!capturing) {
+        const uint64_t adv = std::min<uint64_t>(sweeps, b->total - std::min(b->total, b->hostDone));
+        b->hostDone += adv;
+        b->pendingSweeps = adv;
+    }
     CU(cudaMemsetAsync(L.queue, 0, sizeof(int32_t), b->ctx->stream));
     CU(launch_anneal(L, b->dbytes, b->fmt, b->score64, b->grid, b->threads, b->smem,
                      b->ctx->stream));
@@ -865,7 +995,7 @@ extern "C" int rfmf_batch_run_graph(rfmf_batch* b, uint64_t sweeps, int launches
         cudaGraph_t graph = nullptr;
         CU(cudaStreamBeginCapture(b->ctx->stream, cudaStreamCaptureModeThreadLocal));
         int rc = RFMF_OK;
-        for (int i = 0; i < launches && rc == RFMF_OK; ++i) rc = enqueue_run(b, sweeps);
+        for (int i = 0; i < launches && rc == RFMF_OK; ++i) rc = enqueue_run(b, sweeps, true);
         const cudaError_t ec = cudaStreamEndCapture(b->ctx->stream, &graph);
         if (rc != RFMF_OK) { if (graph) cudaGraphDestroy(graph); return rc; }
         if (ec != cudaSuccess) return fail(RFMF_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ec));
@@ -875,7 +1005,12 @@ extern "C" int rfmf_batch_run_graph(rfmf_batch* b, uint64_t sweeps, int launches
         b->graphSweeps = sweeps;
         b->graphLaunches = launches;
     }
-    for (int r = 0; r < replays; ++r) CU(cudaGraphLaunch(b->graphExec, b->ctx->stream));
+    for (int r = 0; r < replays; ++r) {
+        CU(cudaGraphLaunch(b->graphExec, b->ctx->stream));
+        for (int i = 0; i < launches; ++i)
+            b->hostDone += std::min<uint64_t>(sweeps, b->total - std::min(b->total, b->hostDone));
+    }
+    b->pendingSweeps = 0;   // item times of replayed launches are not harvested
     return RFMF_OK;
 }
 
@@ -910,6 +1045,7 @@ extern "C" int rfmf_batch_synchronize(rfmf_batch* b) {
     if (!b) return fail(RFMF_ERR_INVALID, "batch is NULL");
     CU(cudaSetDevice(b->ctx->device));
     CU(cudaStreamSynchronize(b->ctx->stream));
+    if (int rc = harvest_item_times(*b)) return rc;
     int32_t ctl[4];
     CU(cudaMemcpy(ctl, b->dCtl.p, sizeof ctl, cudaMemcpyDeviceToHost));
     if (ctl[1] != kDevOk) {
@@ -962,6 +1098,7 @@ extern "C" int rfmf_batch_info(const rfmf_batch* b, rfmf_batch_plan* out) {
     out->csr_format = b->fmt + 1;
     out->gain_width = b->dbytes;
     out->smem_bytes = static_cast<int>(b->smem);
+    out->balanced = b->balanced ? 1 : 0;
     return RFMF_OK;
 }
 

@@ -216,3 +216,32 @@ def test_golden_anneal_fixtures(rfmf, ctx):
         assert [int(x) for x in res.final_vals] == case["final"]
         assert [psha(x) for x in res.best_spins] == case["best_partition_sha256"]
         assert [psha(x) for x in res.end_spins] == case["final_partition_sha256"]
+
+
+def _refkernel_cases():
+    import json
+    from conftest import GOLDEN
+    p = GOLDEN / "refkernel_runs.json"
+    return json.loads(p.read_text())["cases"] if p.exists() else []
+
+
+@pytest.mark.parametrize("case", _refkernel_cases(), ids=lambda c: c["name"])
+def test_matches_reference_kernel_fixtures(rfmf, ctx, case):
+    """librfmf.so reproduces runs of the reference's own mcKernel (recorded on
+    a GB300 by tests/golden/make_refkernel_golden.py) bit for bit."""
+    import hashlib
+    import sys
+    sys.path.insert(0, str(__import__("conftest").ROOT / "tests" / "golden"))
+    import make_refkernel_golden as M
+
+    g = M.build_graph(case["graph"] if case["graph"] == "weighted300" else tuple(case["graph"]))
+    h = hashlib.sha256(g.offsets.tobytes() + g.col.tobytes() + g.weight.tobytes()).hexdigest()
+    assert h == case["csr_sha256"]
+    init, solver = chains_for(g, case["seeds"])
+    dg = rfmf.DeviceGraph(ctx, g)
+    res = rfmf.anneal_gpu(ctx, dg, g.max_weighted_degree(), init, case["t0s"], case["phases"],
+                          case["iters"], solver)
+    assert [int(x) for x in res.best_vals] == case["best"]
+    assert [int(x) for x in res.final_vals] == case["final"]
+    assert [M.psha(x) for x in res.best_spins] == case["best_partition_sha256"]
+    assert [M.psha(x) for x in res.end_spins] == case["final_partition_sha256"]
