@@ -210,6 +210,39 @@ int rfmf_batch_info(const rfmf_batch* b, rfmf_batch_plan* out);
 
 int rfmf_batch_destroy(rfmf_batch* b);
 
+/*
+ * The annealer for callers that cannot allocate device memory.  No reference
+ * counterpart: an addition for hosts whose allocator owns all device memory,
+ * code that must not allocate (or synchronise) in the middle of its work, and
+ * embedders that hand the library pre-sized buffers.  It allocates nothing:
+ * inputs and outputs are the caller's device buffers, and the kernel's
+ * scratch (chain records, work items, queue head, error word) lives in a
+ * fixed 640 KiB file-scope device array that every GPU loading this library
+ * holds until the process exits.
+ *
+ * Limits: C <= 4096 chains, nphases <= 64 (RFMF_ERR_CAPACITY beyond).
+ * Inputs (device): d_offsets[n+1] (uint32), d_edges[2 * offsets[n]] as
+ * {int32 col, int32 weight} pairs (the symmetric, row-sorted CSR that
+ * rfmf_csr_validate accepts), d_beta_end / d_beta_val (the run tables of
+ * rfmf_beta_tables for these t0s over the executed sweeps), d_spin_bits
+ * (C * ceil(n/32) words, bit v of chain c = spin +1; overwritten with the
+ * final spins).  Host: t0s, solver_seeds, phases, iters, chain_beta_off
+ * (first run of each chain's table), chain_beta_runs (its run count), and
+ * max_weighted_deg = the graph's true B.  Outputs (device): d_best_bits
+ * (same layout), d_cur / d_best (C int64 each).  Synchronous on `stream`
+ * (a cudaStream_t, NULL for the legacy default stream).  The first call on a
+ * device looks up the array's address and should come before any stream
+ * capture; the array is shared by all calls, which clear what they need, and
+ * calls that overlap on the GPU race on it.
+ */
+int rfmf_anneal_noalloc(int device, void* stream, int64_t n, const uint32_t* d_offsets,
+                        const int32_t* d_edges, int64_t max_weighted_deg, int64_t C,
+                        const double* t0s, const uint64_t* solver_seeds, int64_t nphases,
+                        const uint64_t* phases, const uint64_t* iters, const int64_t* d_beta_end,
+                        const int32_t* d_beta_val, const int64_t* chain_beta_off,
+                        const int64_t* chain_beta_runs, uint32_t* d_spin_bits,
+                        uint32_t* d_best_bits, int64_t* d_cur, int64_t* d_best);
+
 #ifdef __cplusplus
 }
 #endif

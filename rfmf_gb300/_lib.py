@@ -44,6 +44,8 @@ SIGNATURES = [
     ("rfmf_batch_read", ct.c_int, [_P, _P, _P, _P, _P, _P]),
     ("rfmf_batch_info", ct.c_int, [_P, _P]),
     ("rfmf_batch_destroy", ct.c_int, [_P]),
+    ("rfmf_anneal_noalloc", ct.c_int, [ct.c_int, _P, _I64, _P, _P, _I64, _I64, _P, _P, _I64,
+                                       _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
 ]
 
 

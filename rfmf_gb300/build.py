@@ -19,7 +19,7 @@ INCLUDE = PKG.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-Wall", "-I", str(INCLUDE), "-I", str(CSRC)]
-SOURCES = ["rfmf_anneal.cu", "rfmf_driver.cpp"]
+SOURCES = ["rfmf_anneal.cu", "rfmf_driver.cpp", "rfmf_noalloc.cu"]
 
 
 def nvcc():

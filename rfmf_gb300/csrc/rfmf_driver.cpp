@@ -263,6 +263,11 @@ struct rfmf_batch {
     ~rfmf_batch() { if (graphExec) cudaGraphExecDestroy(graphExec); }
 };
 
+// Error channel shared with the other translation units of the library.
+namespace rfmf {
+int set_last_error(int code, const char* msg) { return fail(code, "%s", msg); }
+}  // namespace rfmf
+
 // ------------------------------------------------------------------ misc
 extern "C" const char* rfmf_version(void) { return "rfmf_gb300 0.1 (sm_103a)"; }
 extern "C" const char* rfmf_last_error(void) { return g_err.c_str(); }
