@@ -12,8 +12,11 @@ The expected values (cuts and sha256 of the partition strings, never the
 graphs) are written to tests/golden/committed_log_pin.json together with the
 oracle's outcome, so the pin is on record without the reference present.
 
-Usage: pin_committed_logs.py RESULTS_DIR GRAPH CHAIN[,CHAIN...] [--threads N]
+Usage: pin_committed_logs.py RESULTS_DIR GRAPH CHAIN[,CHAIN...]|all [--threads N]
   e.g. pin_committed_logs.py V100-SXM2-10M G62 0,1,2,3
+With --spec OUT.json it runs nothing: it appends the selected chains' run
+parameters and expected values (cuts, partition hashes) to OUT.json, the input
+of tests/golden/pin_committed_logs_gpu.py, which reruns them on the GPU.
 """
 import argparse
 import ctypes as ct
@@ -64,13 +67,39 @@ def sha(s):
     return hashlib.sha256(s.encode()).hexdigest()
 
 
+def expected_of(chain):
+    return dict(best=chain["best"], final=chain["final"],
+                best_partition_sha256=sha(chain["best_partition"]),
+                final_partition_sha256=sha(chain["final_partition"]))
+
+
+def write_spec(a):
+    rdir = REF / "results" / a.results
+    seeds, t0s, phases, iters = parse_reproduce(rdir / "reproduce.sh", a.graph)
+    log = parse_log(rdir / "logs" / f"{a.graph}.out")
+    sel = range(len(log)) if a.chains == "all" else [int(x) for x in a.chains.split(",")]
+    out = pathlib.Path(a.spec)
+    spec = json.loads(out.read_text()) if out.exists() else {"chains": []}
+    for c in sel:
+        assert log[c]["seed"] == seeds[c] and log[c]["t0"] == t0s[c]
+        spec["chains"].append(dict(results=a.results, graph=a.graph, chain=c, seed=seeds[c],
+                                   t0=t0s[c], phases=phases, iters=iters,
+                                   expected=expected_of(log[c])))
+    out.write_text(json.dumps(spec) + "\n")
+    print(f"{len(sel)} chains of {a.results}/{a.graph} -> {out}")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("results")
     ap.add_argument("graph")
     ap.add_argument("chains")
     ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--spec", default=None)
     a = ap.parse_args()
+    if a.spec:
+        return write_spec(a)
 
     sys.path.insert(0, str(HERE))
     import oracle as ora
@@ -110,14 +139,13 @@ def main():
     best, spins, bestv, cur = res["best_spins"], res["end_spins"], res["best_vals"], res["cur_vals"]
 
     record = json.loads(OUT.read_text()) if OUT.exists() else {"entries": []}
+    record.setdefault("entries", [])
     for k, c in enumerate(sel):
         bp = "".join("0" if s < 0 else "1" for s in best[k])
         fp = "".join("0" if s < 0 else "1" for s in spins[k])
         e = dict(results=a.results, graph=a.graph, chain=c, seed=seeds[c], t0=t0s[c],
                  phases=phases, iters=iters, n=n, m=m,
-                 expected=dict(best=log[c]["best"], final=log[c]["final"],
-                               best_partition_sha256=sha(log[c]["best_partition"]),
-                               final_partition_sha256=sha(log[c]["final_partition"])),
+                 expected=expected_of(log[c]),
                  oracle=dict(best=int(bestv[k]), final=int(cur[k]),
                              best_partition_sha256=sha(bp), final_partition_sha256=sha(fp),
                              seconds=round(el, 1)))

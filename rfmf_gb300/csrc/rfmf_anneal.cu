@@ -302,7 +302,6 @@ struct ChainSmem {
     int32_t* ids;                // int64 mode: winner id per group
     int32_t* win;                // winners of the current sweep
     int64_t* red;                // one partial per warp of the group
-    int32_t* tk;                 // compact-key Gumbel table of this chain
 };
 
 __device__ __forceinline__ ChainSmem carve_chain(unsigned char* base, const DevLaunch& L,
@@ -318,7 +317,6 @@ __device__ __forceinline__ ChainSmem carve_chain(unsigned char* base, const DevL
     s.ids = reinterpret_cast<int32_t*>(base + c.ids);
     s.win = reinterpret_cast<int32_t*>(base + c.win);
     s.red = reinterpret_cast<int64_t*>(base + c.red);
-    s.tk = reinterpret_cast<int32_t*>(base + c.tk);
     return s;
 }
 
@@ -396,12 +394,22 @@ __device__ __forceinline__ unsigned long long warp_max_key(unsigned long long k)
 //   gum * 2^kb = LUT[i] * 2^kb + (f >> 4) * 2^kb
 //              = (LUT[i] * 2^kb - i * 2^(kb-4)) + f * 2^(kb-4)     (kb >= 4)
 // so key = TK[i] + f * 2^(kb-4) + (beta * 2^kb) * delta + (2^kb - 1 - k) with a
-// per-chain 16-entry table TK.  The host enables this path only when
+// 16-entry table TK.  The host enables this path only when
 // (betaMax * B + max|gum| + 1) * 2^kb < 2^31 for every chain, so every key and
 // partial sum is exact in int32; otherwise the launch takes the int64 path.
+//
+// Instruction budget per vertex: TK lives in a register (lane L holds
+// TK[L & 15]) and is read with one shuffle whose source lane is the Philox
+// word itself (a shuffle takes its source lane modulo 32, and lanes L and
+// L + 16 hold the same entry, so the low word needs no masking and the high
+// one a single shift); the field's multiple f * 2^(kb-4) is one multiply-add
+// on the FMA pipe (a mul.hi for the high half-word, whose field sits at bit
+// 16); the final add and max fuse into one add-max.
 struct KeyCfg {
     int kb;          // bits of the block-iteration field
-    int fshift;      // kb - 4
+    uint32_t mulF;   // 2^(kb-4): f * mulF for a low-half field
+    uint32_t mulHi;  // 2^(kb+12): umulhi(x & 0x07FF0000, mulHi) = f * 2^(kb-4)
+    int32_t tkLane;  // TK[lane & 15]
 };
 
 __device__ __forceinline__ int key_bits(int n, int T) {
@@ -411,32 +419,48 @@ __device__ __forceinline__ int key_bits(int n, int T) {
     return kb;
 }
 
+__device__ __forceinline__ KeyCfg key_cfg(int n, int T, int t, const int32_t* lut) {
+    KeyCfg kc;
+    kc.kb = key_bits(n, T);
+    kc.mulF = 1u << (kc.kb - 4);
+    kc.mulHi = 1u << (kc.kb + 12);
+    const int i = t & 15;
+    kc.tkLane = lut[i] * (1 << kc.kb) - i * static_cast<int32_t>(kc.mulF);
+    return kc;
+}
+
+__device__ __forceinline__ uint32_t umulhi_add(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t r;
+    asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+    return r;
+}
+
+// Keys of one block's 8 vertices folded into acc; lanes j >= lim are skipped
+// (the shuffles still run on every lane: the caller keeps the warp converged).
+template <bool kMasked>
 __device__ __forceinline__ void score8_key(int32_t acc[8], const uint32_t x[4], const int32_t d[8],
-                                           int32_t betaK, int32_t ck, int fshift,
-                                           const int32_t* tk, int lim) {
+                                           int32_t betaK, int32_t ck, const KeyCfg& kc, int lim) {
 #pragma unroll
     for (int w = 0; w < 4; ++w) {
-        const uint32_t f0 = x[w] & 0x7FFu;
-        const uint32_t f1 = (x[w] >> 16) & 0x7FFu;
-        if (2 * w < lim) {
-            const int32_t k0 = tk[f0 & 15u] + static_cast<int32_t>(f0 << fshift) +
-                               betaK * d[2 * w] + ck;
-            acc[2 * w] = max(acc[2 * w], k0);
-        }
-        if (2 * w + 1 < lim) {
-            const int32_t k1 = tk[f1 & 15u] + static_cast<int32_t>(f1 << fshift) +
-                               betaK * d[2 * w + 1] + ck;
-            acc[2 * w + 1] = max(acc[2 * w + 1], k1);
-        }
+        const int32_t tk0 = __shfl_sync(0xFFFFFFFFu, kc.tkLane, static_cast<int>(x[w]));
+        const int32_t tk1 = __shfl_sync(0xFFFFFFFFu, kc.tkLane, static_cast<int>(x[w] >> 16));
+        const int32_t f0 = static_cast<int32_t>((x[w] & 0x7FFu) * kc.mulF) + ck;
+        const int32_t f1 = static_cast<int32_t>(
+            umulhi_add(x[w] & 0x07FF0000u, kc.mulHi, static_cast<uint32_t>(ck)));
+        const int32_t k0 = betaK * d[2 * w] + tk0;
+        const int32_t k1 = betaK * d[2 * w + 1] + tk1;
+        if (!kMasked || 2 * w < lim) acc[2 * w] = __viaddmax_s32(k0, f0, acc[2 * w]);
+        if (!kMasked || 2 * w + 1 < lim) acc[2 * w + 1] = __viaddmax_s32(k1, f1, acc[2 * w + 1]);
     }
 }
 
 template <class DP>
-__device__ void select32(const ChainSmem& s, const int32_t* lut, const int32_t* tk,
-                         const KeyCfg& kc, int n, const PhaseCfg& pc, int32_t beta,
-                         uint64_t step, const ChainKeys& keys, int t, int T) {
+__device__ void select32(const ChainSmem& s, const int32_t* lut, const KeyCfg& kc, int n,
+                         const PhaseCfg& pc, int32_t beta, uint64_t step, const ChainKeys& keys,
+                         int t, int T) {
     const SweepConst sc = make_sweep(step, keys);
     const int nfull = n >> 3;
+    const int nblk = (n + 7) >> 3;
     const int P = pc.P;
     const int M = (1 << kc.kb) - 1;
     if (pc.mode != 2) {
@@ -444,32 +468,29 @@ __device__ void select32(const ChainSmem& s, const int32_t* lut, const int32_t* 
         int32_t acc[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) acc[j] = INT32_MIN;
+        // Trip counts are uniform over each warp (its blocks at step k are
+        // wb + kT .. wb + kT + 31), so the table shuffles run converged.
+        const int wb = t & ~31;
         int b = t, k = 0;
-        for (; b + T < nfull; b += 2 * T, k += 2) {
+        for (; wb + T + 31 < nfull - k * T; b += 2 * T, k += 2) {
             uint32_t xa[4], xb[4];
             int32_t da[8], db[8];
             philox_block(static_cast<uint32_t>(b), sc, keys, xa);
             philox_block(static_cast<uint32_t>(b + T), sc, keys, xb);
             DP::load8(s.D, b, da);
             DP::load8(s.D, b + T, db);
-            score8_key(acc, xa, da, betaK, M - k, kc.fshift, tk, 8);
-            score8_key(acc, xb, db, betaK, M - k - 1, kc.fshift, tk, 8);
+            score8_key<false>(acc, xa, da, betaK, M - k, kc, 8);
+            score8_key<false>(acc, xb, db, betaK, M - k - 1, kc, 8);
         }
-        if (b < nfull) {
+        for (; wb + k * T < nblk; b += T, ++k) {
+            // Tail: blocks past the last one are clamped and masked out.
+            const int bb = (b < nblk) ? b : nblk - 1;
+            const int lim = (b < nfull) ? 8 : ((b == nfull) ? (n & 7) : 0);
             uint32_t xa[4];
             int32_t da[8];
-            philox_block(static_cast<uint32_t>(b), sc, keys, xa);
-            DP::load8(s.D, b, da);
-            score8_key(acc, xa, da, betaK, M - k, kc.fshift, tk, 8);
-            b += T;
-            ++k;
-        }
-        if ((n & 7) && b == nfull) {
-            uint32_t xa[4];
-            int32_t da[8];
-            philox_block(static_cast<uint32_t>(b), sc, keys, xa);
-            DP::load8(s.D, b, da);
-            score8_key(acc, xa, da, betaK, M - k, kc.fshift, tk, n & 7);
+            philox_block(static_cast<uint32_t>(bb), sc, keys, xa);
+            DP::load8(s.D, bb, da);
+            score8_key<true>(acc, xa, da, betaK, M - k, kc, lim);
         }
         // Back to (score, v) as a packed 64-bit key for the group reduction.
         unsigned long long key[8];
@@ -650,10 +671,7 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
         s.slots[i] = kS64 ? static_cast<unsigned long long>(LLONG_MIN) : 0ull;
         s.ids[i] = INT32_MAX;
     }
-    KeyCfg kc;
-    kc.kb = key_bits(n, T);
-    kc.fshift = kc.kb - 4;
-    if (t < 16) s.tk[t] = lut[t] * (1 << kc.kb) - t * (1 << kc.fshift);
+    const KeyCfg kc = key_cfg(n, T, t, lut);
     group_sync(grp, T);
     const int nPad = (n + 7) & ~7;
     for (int v = t; v < nPad; v += T)
@@ -746,7 +764,7 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
         const uint64_t step = sw + 1;   // 1-based sweep id
 
         if constexpr (kS64) select64<DP>(s, lut, n, pc, beta, step, keys, t, T, grp);
-        else select32<DP>(s, lut, s.tk, kc, n, pc, beta, step, keys, t, T);
+        else select32<DP>(s, lut, kc, n, pc, beta, step, keys, t, T);
         group_sync(grp, T);
 
         // ---- FLIP 1: winners; negate their gains, flip their spins

@@ -130,10 +130,10 @@ RFMF_HD uint32_t align16(uint32_t x) { return (x + 15u) & ~15u; }
 // Per-chain shared-memory region, in order: gains D (nPad * dbytes), spin
 // bits, best-spin bits, spins as bytes (0/1, for one-load neighbour lookups
 // in FLIP), group key slots (8 B), ids (4 B), winners (4 B),
-// reduction partials (8 B per warp), compact-key Gumbel table (16 x 4 B).
+// reduction partials (8 B per warp).
 // Host and kernel both carve with this.
 struct ChainLayout {
-    uint32_t d, bits, best, sb, slots, ids, win, red, tk, total;
+    uint32_t d, bits, best, sb, slots, ids, win, red, total;
 };
 
 RFMF_HD ChainLayout chain_layout(int maxN, int maxWords, int pmax, int warps, int dbytes) {
@@ -148,7 +148,6 @@ RFMF_HD ChainLayout chain_layout(int maxN, int maxWords, int pmax, int warps, in
     c.ids = o;   o = align16(o + static_cast<uint32_t>(pmax) * 4u);
     c.win = o;   o = align16(o + static_cast<uint32_t>(pmax) * 4u);
     c.red = o;   o = align16(o + static_cast<uint32_t>(warps) * 8u);
-    c.tk = o;    o = align16(o + 16u * 4u);
     c.total = o;
     return c;
 }

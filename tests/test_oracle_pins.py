@@ -71,3 +71,17 @@ def test_committed_log_pin_record():
         assert e["match"], e
         assert e["expected"]["best"] == e["oracle"]["best"]
         assert e["expected"]["best_partition_sha256"] == e["oracle"]["best_partition_sha256"]
+
+
+def test_committed_log_gpu_pin_record():
+    """Record of tests/golden/pin_committed_logs_gpu.py: whole result logs of
+    the reference (every chain of a graph, 8e7 sweeps each) rerun through
+    librfmf.so on a GB300; each chain's cuts and partitions must equal the
+    committed ones."""
+    p = GOLDEN / "committed_log_pin.json"
+    rec = json.loads(p.read_text()) if p.exists() else {}
+    if not rec.get("gpu_entries"):
+        pytest.skip("no GPU rerun of the committed logs recorded yet")
+    for e in rec["gpu_entries"]:
+        assert e["match"], e
+        assert e["gpu"] == e["expected"]
