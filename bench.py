@@ -255,7 +255,7 @@ def gpu_arm(args, rank, world):
     torch.cuda.synchronize()
     clocks.start()
     t_wall = time.perf_counter()
-    step_ms, step_bytes = [], []
+    step_ms, step_bytes, best_by_step = [], [], []
     imp_prev = np.zeros(len(graphs) * args.chains, np.uint64)
     for k in range(K):
         flush.zero_()
@@ -268,6 +268,9 @@ def gpu_arm(args, rank, world):
         ns = np.concatenate([[g.n] * args.chains for g in graphs])
         step_bytes.append(window_bytes(gc, phases, iters, k * per_step, (k + 1) * per_step) +
                           float(np.dot(ns, d_imp)))
+        bv = b.best_vals()
+        best_by_step.append([int(bv[i * args.chains:(i + 1) * args.chains].max())
+                             for i in range(len(graphs))])
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall
     clk = clocks.stop()
@@ -288,6 +291,15 @@ def gpu_arm(args, rank, world):
         assert out["best_vals"][i] == g.cut_value(out["best_spins"][i])
     b.close()
 
+    # time-to-target: target = each graph's best cut at the end of the anneal;
+    # first step boundary at which the running best over its chains reaches it
+    tt = []
+    for i, g in enumerate(graphs):
+        target = best_by_step[-1][i]
+        k_hit = next(k for k in range(K) if best_by_step[k][i] >= target)
+        tt.append({"graph": g.name, "target_cut": target, "sweeps": (k_hit + 1) * per_step,
+                   "seconds": sum(step_ms[:k_hit + 1]) / 1e3})
+
     # e2e through the drop-in call with host buffers
     e2e = None
     if not args.no_e2e:
@@ -295,6 +307,13 @@ def gpu_arm(args, rank, world):
     plain = None
     if not args.no_plain:
         plain = plain_kernel_arm(graphs, setup, args.plain_sweeps, ctx)
+    if plain and "value" in plain:
+        # identical trajectories: the plain kernel needs the same sweeps; its
+        # time follows from its measured chain-steps/s on this workload
+        for e in tt:
+            e["plain_seconds_est"] = e["sweeps"] * len(graphs) * args.chains / plain["value"]
+    batched = None if args.no_batched else batched_arm(args, ctx)
+    serving = None if args.no_serving else serving_arm(args, ctx)
 
     peaks = measured_peaks()
     sm_count = ctx.info()["sm_count"]
@@ -338,6 +357,9 @@ def gpu_arm(args, rank, world):
         "gpu_launches": K,
         "e2e": e2e,
         "plain_kernel": plain,
+        "time_to_target": tt,
+        "batched": batched,
+        "serving": serving,
         "clocks": clk,
         "roofline": {
             "bound": "smem",
@@ -403,6 +425,194 @@ def plain_kernel_arm(graphs, setup, sweeps, ctx):
                     "cudaEvent time, one graph per launch as the reference runs"}
 
 
+def batched_graphs(count, seed=0):
+    """Uneven graphs for the batched form: sizes log-uniform in [800, 20000],
+    families 1/3 each (Erdos-Renyi with mean degree 5-48, toroidal grid,
+    random planar-like with mean degree ~11.7), weights +-1 or +1 alternating."""
+    import math
+
+    import rfmf_gb300 as R
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(800), math.log(20000)))))
+        signed = bool(i % 2)
+        fam = i % 3
+        if fam == 0:
+            g = R.erdos_renyi_sparse(n, float(rng.uniform(5, 48)), signed=signed, seed=1000 + i,
+                                     name=f"er{n}")
+        elif fam == 1:
+            rows = max(3, int(math.sqrt(n)))
+            g = R.torus(rows, max(3, n // rows), signed=signed, seed=1000 + i,
+                        name=f"torus{rows}x{max(3, n // rows)}")
+        else:
+            g = R.planar_like(n, 11.7, signed=signed, seed=1000 + i, name=f"planar{n}")
+        out.append(g)
+    return out
+
+
+def batched_arm(args, ctx):
+    """The batched form against the plain kernel on the same sample: G uneven
+    graphs x 64 chains in ONE persistent launch (work queue over graphs,
+    CTA shape and chains per CTA from the planner), vs the reference's kernel
+    launched once per graph as it runs.  Both advance every chain the same
+    sweeps; results must be identical chain for chain."""
+    import torch
+
+    import rfmf_gb300 as R
+    sys.path.insert(0, str(ROOT / "oracle"))
+    t = time.perf_counter()
+    graphs = batched_graphs(args.batched_graphs)
+    gen_s = time.perf_counter() - t
+    C = 64
+    sweeps = args.batched_sweeps
+    phases, iters = schedule(sweeps)
+    dgs = [R.DeviceGraph(ctx, g) for g in graphs]
+    setup = []
+    for i, g in enumerate(graphs):
+        seeds = [5_000_000 + C * i + k for k in range(C)]
+        setup.append(dict(init=np.stack([R.initial_spins(x, g.n) for x in seeds]),
+                          solver=[R.solver_seed(x) for x in seeds],
+                          t0s=[LADDER[k % 8] for k in range(C)]))
+    gl, ini, sol, t0 = [], [], [], []
+    for dg, st in zip(dgs, setup):
+        gl += [dg] * C
+        ini += list(st["init"])
+        sol += st["solver"]
+        t0 += st["t0s"]
+    # warm-up batch (learned per-graph costs feed the work-item sizing)
+    wb = R.Batch(ctx, gl, t0, sol, ini, phases, iters)
+    wb.run_timed(min(sweeps, 2000))
+    wb.close()
+    b = R.Batch(ctx, gl, t0, sol, ini, phases, iters)
+    ms = b.run_timed(sweeps)
+    info = b.info()
+    out = b.read()
+    b.close()
+    chain_steps = len(graphs) * C * sweeps
+    res = {"value": chain_steps / (ms / 1e3), "unit": "chain-steps/s", "graphs": len(graphs),
+           "chains_per_graph": C, "sweeps": sweeps, "launches": 1, "kernel_ms": ms,
+           "plan": {k: info[k] for k in ("threads_per_chain", "chains_per_cta", "grid", "items",
+                                         "csr_format", "gain_width", "balanced")},
+           "n_range": [min(g.n for g in graphs), max(g.n for g in graphs)],
+           "graph_gen_s": gen_s}
+    try:
+        import refgpu
+    except Exception as e:   # pragma: no cover
+        res["plain_kernel"] = {"unavailable": f"harness import failed: {e}"}
+        return res
+    if not refgpu.available():
+        res["plain_kernel"] = {"unavailable": "reference kernel cubin (oracle/_ref) not built"}
+        return res
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    ref_ms = 0.0
+    same = True
+    for i, (g, st) in enumerate(zip(graphs, setup)):
+        r = refgpu.run(g, st["init"], st["t0s"], st["solver"], phases, iters, sms)
+        ref_ms += r["ms"]
+        mine_best = np.stack(out["best_spins"][i * C:(i + 1) * C])
+        mine_end = np.stack(out["end_spins"][i * C:(i + 1) * C])
+        same = same and np.array_equal(mine_best, r["best_spins"]) and \
+            np.array_equal(mine_end, r["end_spins"]) and \
+            np.array_equal(out["best_vals"][i * C:(i + 1) * C], r["best_vals"])
+    plain = chain_steps / (ref_ms / 1e3)
+    res["plain_kernel"] = {"value": plain, "unit": "chain-steps/s", "launches": len(graphs),
+                           "kernel_ms": ref_ms, "identical_results": bool(same),
+                           "what": "reference mcKernel (sm_103a build of its sources), one "
+                                   "launch per graph, kernel-only cudaEvent time"}
+    res["speedup_vs_plain"] = res["value"] / plain
+    if not same:
+        raise AssertionError("batched results differ from the reference kernel")
+    return res
+
+
+def serving_graphs():
+    import rfmf_gb300 as R
+    out = []
+    for k, n in enumerate((5000, 10000, 20000)):
+        rows = int(n ** 0.5)
+        out.append(R.torus(rows, n // rows, signed=True, seed=k, name=f"torus{rows}x{n // rows}"))
+        out.append(R.random_tree(n, seed=k, name=f"tree{n}"))
+        out.append(R.erdos_renyi_sparse(n, 5, signed=True, seed=k, name=f"er{n}_d5"))
+    return out
+
+
+def serving_arm(args, ctx):
+    """Continuous batching through the request server: Poisson arrivals at
+    `rate` req/s for `seconds`; each request draws a graph from the
+    large-sparse families (torus, tree, ER d=5; n 5000-20000), 16-256 chains
+    and a budget of args.serve_sweeps sweeps (default schedule).  Latency =
+    submit -> results on the host (server clock)."""
+    import threading
+
+    import rfmf_gb300 as R
+    graphs = serving_graphs()
+    dgs = [R.DeviceGraph(ctx, g) for g in graphs]
+    rng = np.random.default_rng(17)
+    rate, seconds = args.serve_rate, args.serve_seconds
+    arrivals = []
+    t = 0.0
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t > seconds:
+            break
+        arrivals.append(t)
+    reqs = [dict(g=int(rng.integers(len(graphs))), C=int(rng.choice([16, 32, 64, 128, 256])),
+                 seed0=10_000_000 + 1000 * i) for i in range(len(arrivals))]
+    phases, iters = schedule(args.serve_sweeps)
+    srv = R.Server(ctx, window_sweeps=args.serve_window)
+    ids = [None] * len(reqs)
+    err = []
+
+    def submitter():
+        t0 = time.perf_counter()
+        for i, (at, r) in enumerate(zip(arrivals, reqs)):
+            g = graphs[r["g"]]
+            seeds = [r["seed0"] + k for k in range(r["C"])]
+            init = np.stack([R.initial_spins(x, g.n) for x in seeds])
+            d = at - (time.perf_counter() - t0)
+            if d > 0:
+                time.sleep(d)
+            try:
+                ids[i] = srv.submit(dgs[r["g"]], init, [LADDER[k % 8] for k in range(r["C"])],
+                                    phases, iters, [R.solver_seed(x) for x in seeds])
+            except Exception as e:   # pragma: no cover
+                err.append(repr(e))
+                return
+
+    th = threading.Thread(target=submitter)
+    t_start = time.perf_counter()
+    th.start()
+    th.join()
+    if err:
+        raise RuntimeError(err[0])
+    lat, cs = [], 0
+    for i, r in enumerate(reqs):
+        st = srv.wait(ids[i], timeout=600)
+        if st["state"] != "done":
+            raise RuntimeError(f"request {i} {st['state']}")
+        lat.append(st["finish_s"] - st["submit_s"])
+        res = srv.result(ids[i])
+        g = graphs[r["g"]]
+        if res.best_vals[0] != g.cut_value(res.best_spins[0]):
+            raise AssertionError("served best cut disagrees with its spins")
+        cs += r["C"] * args.serve_sweeps
+    wall = time.perf_counter() - t_start
+    stats = srv.stats()
+    srv.close()
+    lat = np.array(lat)
+    return {"rate_req_s": rate, "requests": len(reqs), "duration_s": seconds,
+            "sweeps_per_request": args.serve_sweeps, "window_sweeps": args.serve_window,
+            "latency_p50_s": float(np.percentile(lat, 50)),
+            "latency_p99_s": float(np.percentile(lat, 99)),
+            "latency_max_s": float(lat.max()),
+            "chain_steps_per_s": cs / wall, "wall_s": wall,
+            "gpu_busy_frac": stats["kernel_s"] / wall, "windows": stats["windows"],
+            "launches": stats["launches"],
+            "mix": "graphs torus/tree/ER-d5 at n 5000/10000/20000; chains 16-256 uniform over "
+                   "{16,32,64,128,256}; Poisson arrivals"}
+
+
 def e2e_arm(args, ctx, graphs, setup, per_step):
     import rfmf_gb300 as R
     phases, iters = schedule(per_step)
@@ -446,6 +656,14 @@ def main():
     ap.add_argument("--plain-sweeps", type=int, default=16000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-graphs", type=int, default=512)
+    ap.add_argument("--batched-sweeps", type=int, default=2000)
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-rate", type=float, default=2.0)
+    ap.add_argument("--serve-seconds", type=float, default=20.0)
+    ap.add_argument("--serve-sweeps", type=int, default=100_000)
+    ap.add_argument("--serve-window", type=int, default=4096)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))

@@ -210,6 +210,74 @@ int rfmf_batch_info(const rfmf_batch* b, rfmf_batch_plan* out);
 
 int rfmf_batch_destroy(rfmf_batch* b);
 
+/* ---- request server ------------------------------------------------------
+ * Serving form of annealGpu (the reference serves one annealGpu call per
+ * process; proposed in its place: rfmf_submit / rfmf_poll).  A server owns a
+ * worker thread and a stream on the context's device.  Each submitted
+ * request is one annealGpu call's worth of chains (one graph, one schedule,
+ * per-chain t0 and seed).  The worker advances every admitted request's
+ * chains together, `window_sweeps` sweeps per persistent launch (continuous
+ * batching); requests join at the next window boundary and leave when their
+ * chains finish.  Results are bit-identical to rfmf_anneal on the same
+ * inputs.  All calls are thread-safe.  A graph must outlive the requests
+ * that use it. */
+typedef struct rfmf_server rfmf_server;
+
+typedef struct rfmf_server_config {
+    uint64_t window_sweeps;      /* sweeps per launch window (0 = 4096) */
+    int64_t max_chains;          /* chains admitted at once (0 = 1 << 20); later requests queue */
+    rfmf_launch_config launch;   /* threads_per_chain / gain_width / csr_format / score_path */
+} rfmf_server_config;
+
+enum rfmf_request_state {
+    RFMF_REQ_QUEUED = 0,
+    RFMF_REQ_RUNNING = 1,
+    RFMF_REQ_DONE = 2,
+    RFMF_REQ_FAILED = 3
+};
+
+typedef struct rfmf_request_status {
+    int state;                   /* rfmf_request_state */
+    int error;                   /* rfmf_status of a failed request */
+    uint64_t sweeps_done;        /* sweeps every chain of the request has completed */
+    uint64_t sweeps_total;
+    double submit_s;             /* server clock (seconds since create) */
+    double start_s;              /* admitted to the GPU (0 while queued) */
+    double finish_s;             /* results on the host (0 until done) */
+} rfmf_request_status;
+
+typedef struct rfmf_server_stats {
+    uint64_t windows;            /* launch windows run */
+    uint64_t launches;           /* kernel launches (one per launch class per window) */
+    uint64_t chain_sweeps;       /* chain-sweeps completed */
+    double busy_s;               /* wall time inside windows (admission + launches + harvest) */
+    double kernel_s;             /* device time of the launches (CUDA events) */
+    int64_t queued, running, done;   /* requests by state */
+} rfmf_server_stats;
+
+int rfmf_server_create(rfmf_context* ctx, const rfmf_server_config* cfg, rfmf_server** out);
+
+/* Stops the worker after the window in flight; unread results are dropped. */
+int rfmf_server_destroy(rfmf_server* s);
+
+/* Copies the inputs (laid out as for rfmf_anneal) and queues the request. */
+int rfmf_submit(rfmf_server* s, const rfmf_graph* g, int64_t nchains, const int8_t* initial_spins,
+                const double* t0s, int64_t nphases, const uint64_t* phases, const uint64_t* iters,
+                const uint64_t* solver_seeds, uint64_t* request_id);
+
+int rfmf_poll(rfmf_server* s, uint64_t request_id, rfmf_request_status* status);
+
+/* Blocks until the request is done or failed, or timeout_s passes
+ * (timeout_s < 0: no limit); RFMF_ERR_CAPACITY on timeout. */
+int rfmf_wait(rfmf_server* s, uint64_t request_id, double timeout_s, rfmf_request_status* status);
+
+/* Results of a done request (layouts as rfmf_anneal; any pointer may be
+ * NULL); releases the request.  A failed request returns its error. */
+int rfmf_result(rfmf_server* s, uint64_t request_id, int8_t* end_spins, int8_t* best_spins,
+                int64_t* best_vals, int64_t* final_vals);
+
+int rfmf_server_stats_get(rfmf_server* s, rfmf_server_stats* out);
+
 /*
  * The annealer for callers that cannot allocate device memory.  No reference
  * counterpart: an addition for hosts whose allocator owns all device memory,

@@ -46,6 +46,13 @@ SIGNATURES = [
     ("rfmf_batch_destroy", ct.c_int, [_P]),
     ("rfmf_anneal_noalloc", ct.c_int, [ct.c_int, _P, _I64, _P, _P, _I64, _I64, _P, _P, _I64,
                                        _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    ("rfmf_server_create", ct.c_int, [_P, _P, _P]),
+    ("rfmf_server_destroy", ct.c_int, [_P]),
+    ("rfmf_submit", ct.c_int, [_P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P]),
+    ("rfmf_poll", ct.c_int, [_P, _U64, _P]),
+    ("rfmf_wait", ct.c_int, [_P, _U64, ct.c_double, _P]),
+    ("rfmf_result", ct.c_int, [_P, _U64, _P, _P, _P, _P]),
+    ("rfmf_server_stats_get", ct.c_int, [_P, _P]),
 ]
 
 
@@ -65,6 +72,29 @@ class BatchPlan(ct.Structure):
                 ("csr_format", ct.c_int), ("gain_width", ct.c_int), ("smem_bytes", ct.c_int),
                 ("balanced", ct.c_int)]
 
+
+class ServerConfig(ct.Structure):
+    """rfmf_server_config."""
+    _fields_ = [("window_sweeps", ct.c_uint64), ("max_chains", ct.c_int64),
+                ("launch", LaunchConfig)]
+
+
+class RequestStatus(ct.Structure):
+    """rfmf_request_status."""
+    _fields_ = [("state", ct.c_int), ("error", ct.c_int), ("sweeps_done", ct.c_uint64),
+                ("sweeps_total", ct.c_uint64), ("submit_s", ct.c_double),
+                ("start_s", ct.c_double), ("finish_s", ct.c_double)]
+
+
+class ServerStats(ct.Structure):
+    """rfmf_server_stats."""
+    _fields_ = [("windows", ct.c_uint64), ("launches", ct.c_uint64),
+                ("chain_sweeps", ct.c_uint64), ("busy_s", ct.c_double),
+                ("kernel_s", ct.c_double), ("queued", ct.c_int64), ("running", ct.c_int64),
+                ("done", ct.c_int64)]
+
+
+REQUEST_STATES = {0: "queued", 1: "running", 2: "done", 3: "failed"}
 
 STATUS = {0: "RFMF_OK", 1: "RFMF_ERR_INVALID", 2: "RFMF_ERR_CUDA", 3: "RFMF_ERR_NOMEM",
           4: "RFMF_ERR_CAPACITY", 5: "RFMF_ERR_DEVICE", 6: "RFMF_ERR_BETA_RUNS"}

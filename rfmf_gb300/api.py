@@ -11,7 +11,8 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import BatchPlan, LaunchConfig, RfmfError, check, lib
+from ._lib import (REQUEST_STATES, BatchPlan, LaunchConfig, RequestStatus, RfmfError,
+                   ServerConfig, ServerStats, check, lib)
 
 # Offset between a chain's raw seed (initial spins) and its Philox solver seed
 # (src/host_common.h:22-25, main.cu:27-29).
@@ -242,9 +243,93 @@ class Batch:
         return dict(end_spins=np.split(end, splits), best_spins=np.split(best, splits),
                     cur_vals=cur, best_vals=bv, sweeps_done=done)
 
+    def best_vals(self):
+        """Best cut of every chain so far (waits for launches in flight)."""
+        bv = np.zeros(self.C, np.int64)
+        check(lib().rfmf_batch_read(self.h, None, None, None, _p(bv), None))
+        return bv
+
     def close(self):
         if self.h:
             lib().rfmf_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Request server (rfmf_server): continuous batching of annealGpu-sized
+    requests over persistent launches; submit from any thread, poll or wait,
+    then take the results.  Each request's results equal anneal_gpu on the
+    same inputs."""
+
+    def __init__(self, ctx, window_sweeps=4096, max_chains=0, cfg=None):
+        sc = ServerConfig()
+        sc.window_sweeps = int(window_sweeps)
+        sc.max_chains = int(max_chains)
+        sc.launch = cfg or make_config()
+        h = ct.c_void_p()
+        check(lib().rfmf_server_create(ctx.h, ct.byref(sc), ct.byref(h)))
+        self.h = h
+        self.ctx = ctx
+        self._req = {}   # id -> (n, C, graph kept alive)
+
+    def submit(self, dgraph, init_spins, t0s, phases, iters, solver_seeds):
+        spins = np.ascontiguousarray(init_spins, np.int8)
+        C = spins.shape[0]
+        t = np.ascontiguousarray(t0s, np.float64)
+        sd = np.array([int(s) % 2**64 for s in solver_seeds], np.uint64)
+        ph = np.ascontiguousarray(phases, np.uint64)
+        it = np.ascontiguousarray(iters, np.uint64)
+        rid = ct.c_uint64()
+        check(lib().rfmf_submit(self.h, dgraph.h, C, _p(spins), _p(t), len(ph), _p(ph), _p(it),
+                                _p(sd), ct.byref(rid)))
+        self._req[rid.value] = (dgraph.n, C, dgraph)
+        return rid.value
+
+    @staticmethod
+    def _status(st):
+        return dict(state=REQUEST_STATES[st.state], error=st.error, sweeps_done=st.sweeps_done,
+                    sweeps_total=st.sweeps_total, submit_s=st.submit_s, start_s=st.start_s,
+                    finish_s=st.finish_s)
+
+    def poll(self, rid):
+        st = RequestStatus()
+        check(lib().rfmf_poll(self.h, int(rid), ct.byref(st)))
+        return self._status(st)
+
+    def wait(self, rid, timeout=-1.0):
+        st = RequestStatus()
+        check(lib().rfmf_wait(self.h, int(rid), float(timeout), ct.byref(st)))
+        return self._status(st)
+
+    def result(self, rid):
+        """Results of a done request (releases it); raises while it runs."""
+        n, C, _ = self._req[rid]
+        end = np.zeros((C, n), np.int8)
+        best = np.zeros((C, n), np.int8)
+        bv = np.zeros(C, np.int64)
+        fv = np.zeros(C, np.int64)
+        finished = self.poll(rid)["state"] in ("done", "failed")
+        try:
+            check(lib().rfmf_result(self.h, int(rid), _p(end), _p(best), _p(bv), _p(fv)))
+        finally:
+            if finished:
+                self._req.pop(rid, None)
+        return AnnealResult(end, best, 0.0, bv, fv)
+
+    def stats(self):
+        s = ServerStats()
+        check(lib().rfmf_server_stats_get(self.h, ct.byref(s)))
+        return {name: getattr(s, name) for name, _ in ServerStats._fields_}
+
+    def close(self):
+        if self.h:
+            lib().rfmf_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -1,6 +1,6 @@
 """Build librfmf.so (sm_103a) in-tree with nvcc.
 
-The two translation units compile in parallel and link into
+The translation units compile in parallel and link into
 rfmf_gb300/_build/librfmf.so.  No cmake, no torch extension machinery: the
 library is plain C ABI over CUDA, so it builds the same on x86_64 and aarch64.
 """
@@ -19,7 +19,7 @@ INCLUDE = PKG.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-Wall", "-I", str(INCLUDE), "-I", str(CSRC)]
-SOURCES = ["rfmf_anneal.cu", "rfmf_driver.cpp", "rfmf_noalloc.cu"]
+SOURCES = ["rfmf_anneal.cu", "rfmf_driver.cpp", "rfmf_noalloc.cu", "rfmf_server.cpp"]
 
 
 def nvcc():

@@ -740,8 +740,19 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
     PhaseCfg pc = phase_cfg(P, t, T);
 
     const ChainKeys keys = make_keys(ch.solverSeed);
-    uint64_t betaNext = (s1 > s0) ? static_cast<uint64_t>(ch.betaEnd[run]) : 0;
-    int32_t beta = (s1 > s0) ? ch.betaVal[run] : 0;
+    // Beta cursor in registers, with the following run prefetched one run
+    // ahead (read-only path): a run change costs no dependent global load.
+    const int64_t* __restrict__ bEnd = ch.betaEnd;
+    const int32_t* __restrict__ bVal = ch.betaVal;
+    const int64_t nRuns = ch.betaRuns;
+    uint64_t betaNext = (s1 > s0) ? static_cast<uint64_t>(__ldg(bEnd + run)) : 0;
+    int32_t beta = (s1 > s0) ? __ldg(bVal + run) : 0;
+    uint64_t pfEnd = ~0ull;
+    int32_t pfVal = 0;
+    if (s1 > s0 && run + 1 < nRuns) {
+        pfEnd = static_cast<uint64_t>(__ldg(bEnd + run + 1));
+        pfVal = __ldg(bVal + run + 1);
+    }
     uint64_t improved = 0;
     group_sync(grp, T);
 
@@ -757,9 +768,14 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
             pc = phase_cfg(P, t, T);
         }
         if (sw >= betaNext) {
+            // Runs are never empty, so one step of the cursor per sweep.
             ++run;
-            betaNext = static_cast<uint64_t>(ch.betaEnd[run]);
-            beta = ch.betaVal[run];
+            betaNext = pfEnd;
+            beta = pfVal;
+            if (run + 1 < nRuns) {
+                pfEnd = static_cast<uint64_t>(__ldg(bEnd + run + 1));
+                pfVal = __ldg(bVal + run + 1);
+            }
         }
         const uint64_t step = sw + 1;   // 1-based sweep id
 

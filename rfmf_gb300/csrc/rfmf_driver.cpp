@@ -20,18 +20,11 @@
 #include <string>
 #include <vector>
 
-#include "../../include/rfmf.h"
-#include "rfmf_device.h"
-
-namespace rfmf {
-const void* kernel_ptr(int dbytes, int fmt, bool s64);
-cudaError_t launch_anneal(const DevLaunch& L, int dbytes, int fmt, bool s64, int grid,
-                          int threads, size_t smem, cudaStream_t stream);
-}  // namespace rfmf
+#include "rfmf_host.h"
 
 using namespace rfmf;
 
-namespace {
+namespace rfmf {
 
 thread_local std::string g_err;
 
@@ -44,19 +37,6 @@ int fail(int code, const char* fmt, ...) {
     g_err = buf;
     return code;
 }
-
-#define CU(call)                                                                 \
-    do {                                                                         \
-        const cudaError_t e_ = (call);                                           \
-        if (e_ != cudaSuccess)                                                   \
-            return fail(e_ == cudaErrorMemoryAllocation ? RFMF_ERR_NOMEM         \
-                                                        : RFMF_ERR_CUDA,         \
-                        "%s failed: %s", #call, cudaGetErrorString(e_));         \
-    } while (0)
-
-constexpr uint64_t kMaxTotalSteps = 1000000000000ull;   // src/host_common.h:80
-constexpr int64_t kMaxBetaRuns = 33000000;              // src/host_common.h:99
-constexpr int64_t kGumbelMaxMag = 3617486 + 127;        // src/philox.cuh:44-48
 
 // Q20 Gumbel quantile table: round(-log(-log((2i+1)/32)) * 2^20), the
 // defining formula of src/philox.cuh:26-34 (every entry >= 0.016 away from a
@@ -143,13 +123,6 @@ int append_runs(double t0, int64_t total, std::vector<int64_t>& end, std::vector
     }
 }
 
-struct BetaTables {
-    std::vector<int64_t> end;
-    std::vector<int32_t> val;
-    std::vector<int64_t> chainOff;
-    std::vector<int64_t> chainRuns;
-};
-
 int build_beta(const double* t0s, int64_t C, int64_t total, BetaTables& bt) {
     // beta_fixed must stay inside int32: past it the reference's
     // static_cast<int32_t>(round(...)) (src/host_common.h:73-76) is undefined
@@ -190,48 +163,7 @@ bool score_safe_int32(int64_t total, double t0, int64_t B) {
     return (bmf * B + kGumbelMaxMag) < static_cast<int64_t>(std::numeric_limits<int32_t>::max());
 }
 
-// Owning device buffer.
-struct DevBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-    ~DevBuf() { if (p) cudaFree(p); }
-    int alloc(size_t b) {
-        bytes = std::max<size_t>(b, 16);
-        const cudaError_t e = cudaMalloc(&p, bytes);
-        if (e != cudaSuccess) {
-            p = nullptr;
-            return fail(e == cudaErrorMemoryAllocation ? RFMF_ERR_NOMEM : RFMF_ERR_CUDA,
-                        "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
-        }
-        return RFMF_OK;
-    }
-    template <class T> T* as() const { return static_cast<T*>(p); }
-};
-
-}  // namespace
-
-struct rfmf_context {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    int sms = 0;
-    int smemOptin = 0;
-    int32_t lut[16];
-};
-
-// A graph in device memory: offsets and 8-byte entries for HBM walks, plus
-// the compact entry arrays the shared-memory formats stage from (present
-// when the graph qualifies).  All arrays are padded to 16 bytes.
-struct rfmf_graph {
-    rfmf_context* ctx = nullptr;
-    int64_t n = 0, m = 0, B = 0, wsum2 = 0;
-    bool unit16 = false, packed32 = false;
-    uint32_t offBytes = 0, u16Bytes = 0, p32Bytes = 0;
-    DevBuf offsets, edges, u16, p32;
-    // Learned cost: device ns per chain-sweep of one CTA slot, from the item
-    // timings of earlier launches (weight = chain-sweeps observed).  Feeds the
-    // work-item sizing of later launches; never affects results.
-    mutable double costNs = 0.0, costWeight = 0.0;
-};
+}  // namespace rfmf
 
 struct rfmf_batch {
     rfmf_context* ctx = nullptr;
@@ -520,17 +452,7 @@ extern "C" int rfmf_graph_info(const rfmf_graph* g, int64_t* n, int64_t* m, int6
     return RFMF_OK;
 }
 // ------------------------------------------------------------------ batch
-namespace {
-
-// Launch plan: gain width, CSR format, warps per chain W, chains per CTA K.
-//  * gain width: int8 when every graph has B <= 127, else int32;
-//  * CSR format: the most compact shared-memory format every graph supports
-//    (unit16, else packed32), else HBM walks;
-//  * W: one warp per chain unless a chain has enough vertex blocks to keep
-//    more warps busy (about 384 blocks of 8 vertices per extra warp);
-//  * K: the smallest number of chains per CTA that lets every work item be
-//    resident at once (one wave), within shared memory, 512 threads per CTA
-//    and the named-barrier budget; with more chains than that, the largest.
+namespace rfmf {
 // Warps per chain: one unless a chain has enough vertex blocks to keep more
 // warps busy (about 384 blocks of 8 vertices per extra warp).
 int choose_warps(int maxN, const rfmf_launch_config& c) {
@@ -559,6 +481,20 @@ bool compact_key_safe(int64_t total, double t0, int64_t B, int kb) {
                std::ldexp(1.0, kb) < 2147483647.0;
 }
 
+}  // namespace rfmf
+
+namespace {
+
+// Launch plan: gain width, CSR format, warps per chain W, chains per CTA K.
+//  * gain width: int8 when every graph has B <= 127, else int32;
+//  * CSR format: the most compact shared-memory format every graph supports
+//    (unit16, else packed32), else HBM walks;
+//  * W: one warp per chain unless a chain has enough vertex blocks to keep
+//    more warps busy (about 384 blocks of 8 vertices per extra warp);
+//  * K: the smallest number of chains per CTA that lets every work item be
+//    resident at once (one wave), within shared memory, the kernel's CTA
+//    thread limit and the named-barrier budget; with more chains than that,
+//    the largest.
 struct Plan {
     int dbytes, fmt, warps, K, Kuniform, threads, grid, nitems, pmax, occ;
     uint32_t csrBytes, chainBytes;
@@ -596,7 +532,13 @@ int plan_launch(rfmf_batch& b, const std::vector<const rfmf_graph*>& glist,
             for (const rfmf_graph* g : glist)
                 csrBytes = std::max(csrBytes, g->offBytes + (fmt == kCsrUnit16 ? g->u16Bytes : g->p32Bytes));
         const uint32_t chainBytes = chain_layout(maxN, maxWords, pl.pmax, W, pl.dbytes).total;
-        const int kCap = std::min(16 / W, W > 1 ? 15 : 16);
+        const void* k2 = kernel_ptr(pl.dbytes, fmt, b.score64);
+        cudaFuncAttributes fa2{};
+        CU(cudaFuncGetAttributes(&fa2, k2));
+        // Warp groups per CTA: named barriers 1..15, and the variant's
+        // register budget bounds the CTA's threads.
+        const int kCap = std::min(std::min(16 / W, W > 1 ? 15 : 16), fa2.maxThreadsPerBlock / (32 * W));
+        if (kCap < 1) return fail(RFMF_ERR_CAPACITY, "a %d-thread chain exceeds the kernel's CTA limit", 32 * W);
         const int64_t room = dynMax - kSmemHeader - csrBytes;
         int Kmax = room > 0 ? static_cast<int>(std::min<int64_t>(kCap, room / chainBytes)) : 0;
         if (c.chains_per_cta) {
@@ -610,7 +552,6 @@ int plan_launch(rfmf_batch& b, const std::vector<const rfmf_graph*>& glist,
                         "one chain needs %u B of shared memory beside a %u B CSR, but a CTA "
                         "has %lld B", chainBytes, csrBytes, static_cast<long long>(dynMax));
         }
-        const void* k2 = kernel_ptr(pl.dbytes, fmt, b.score64);
         CU(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dynMax)));
         CU(cudaFuncSetAttribute(k2, cudaFuncAttributePreferredSharedMemoryCarveout,
                                 cudaSharedmemCarveoutMaxShared));

@@ -1,0 +1,105 @@
+// rfmf_host.h -- host-side internals shared by the translation units of
+// librfmf.so (the C ABI driver, the request server, the no-alloc entry
+// point).  Not installed; the public interface is include/rfmf.h.
+#ifndef RFMF_HOST_H
+#define RFMF_HOST_H
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/rfmf.h"
+#include "rfmf_device.h"
+
+namespace rfmf {
+
+// Kernel entry points (rfmf_anneal.cu).
+const void* kernel_ptr(int dbytes, int fmt, bool s64);
+cudaError_t launch_anneal(const DevLaunch& L, int dbytes, int fmt, bool s64, int grid,
+                          int threads, size_t smem, cudaStream_t stream);
+
+// Error channel: records the message for rfmf_last_error() (per host thread)
+// and returns `code`.
+int fail(int code, const char* fmt, ...);
+int set_last_error(int code, const char* msg);
+
+#define CU(call)                                                                 \
+    do {                                                                         \
+        const cudaError_t e_ = (call);                                           \
+        if (e_ != cudaSuccess)                                                   \
+            return ::rfmf::fail(e_ == cudaErrorMemoryAllocation ? RFMF_ERR_NOMEM \
+                                                                : RFMF_ERR_CUDA, \
+                                "%s failed: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+constexpr uint64_t kMaxTotalSteps = 1000000000000ull;   // src/host_common.h:80
+constexpr int64_t kMaxBetaRuns = 33000000;              // src/host_common.h:99
+constexpr int64_t kGumbelMaxMag = 3617486 + 127;        // src/philox.cuh:44-48
+
+void gumbel_lut(int32_t lut[16]);
+
+// Run-length beta tables of a set of chains: one table per distinct t0,
+// chain c reads runs [chainOff[c], chainOff[c] + chainRuns[c]).
+struct BetaTables {
+    std::vector<int64_t> end;
+    std::vector<int32_t> val;
+    std::vector<int64_t> chainOff;
+    std::vector<int64_t> chainRuns;
+};
+int build_beta(const double* t0s, int64_t C, int64_t total, BetaTables& bt);
+bool score_safe_int32(int64_t total, double t0, int64_t B);
+
+// Launch-shape helpers of the planner.
+int choose_warps(int maxN, const rfmf_launch_config& c);
+int key_bits(int64_t n, int T);
+bool compact_key_safe(int64_t total, double t0, int64_t B, int kb);
+
+// Owning device buffer.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { if (p) cudaFree(p); }
+    int alloc(size_t b) {
+        bytes = b < 16 ? 16 : b;
+        const cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return fail(e == cudaErrorMemoryAllocation ? RFMF_ERR_NOMEM : RFMF_ERR_CUDA,
+                        "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+        }
+        return RFMF_OK;
+    }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace rfmf
+
+struct rfmf_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int sms = 0;
+    int smemOptin = 0;
+    int32_t lut[16];
+};
+
+// A graph in device memory: offsets and 8-byte entries for HBM walks, plus
+// the compact entry arrays the shared-memory formats stage from (present
+// when the graph qualifies).  All arrays are padded to 16 bytes.
+struct rfmf_graph {
+    rfmf_context* ctx = nullptr;
+    int64_t n = 0, m = 0, B = 0, wsum2 = 0;
+    bool unit16 = false, packed32 = false;
+    uint32_t offBytes = 0, u16Bytes = 0, p32Bytes = 0;
+    rfmf::DevBuf offsets, edges, u16, p32;
+    // Learned cost: device ns per chain-sweep of one CTA slot, from the item
+    // timings of earlier launches (weight = chain-sweeps observed).  Feeds the
+    // work-item sizing of later launches; never affects results.
+    mutable double costNs = 0.0, costWeight = 0.0;
+};
+
+#endif  // RFMF_HOST_H

@@ -173,20 +173,23 @@ extern "C" int rfmf_anneal_noalloc(int device, void* stream, int64_t n,
     if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess) return nerr(RFMF_ERR_CUDA, "kernel attributes");
     const int dynMax = optin - static_cast<int>(fa.sharedSizeBytes);
     const int64_t room = static_cast<int64_t>(dynMax) - kSmemHeader;
-    const int Kmax = static_cast<int>(std::min<int64_t>(16, room / chainBytes));
+    const int Kmax = static_cast<int>(
+        std::min<int64_t>(std::min(16, fa.maxThreadsPerBlock / (32 * W)), room / chainBytes));
     if (Kmax < 1) return nerr(RFMF_ERR_CAPACITY, "chain state does not fit shared memory");
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dynMax) != cudaSuccess)
         return nerr(RFMF_ERR_CUDA, "kernel attribute");
     int K = Kmax, occ = 0;
     for (int k = 1; k <= Kmax; ++k) {
+        int o = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &occ, kern, 32 * W * k, kSmemHeader + static_cast<size_t>(k) * chainBytes) != cudaSuccess ||
-            occ <= 0) {
+                &o, kern, 32 * W * k, kSmemHeader + static_cast<size_t>(k) * chainBytes) != cudaSuccess ||
+            o <= 0) {
             cudaGetLastError();
             continue;
         }
         K = k;
-        if ((C + k - 1) / k <= static_cast<int64_t>(occ) * sms) break;
+        occ = o;
+        if ((C + k - 1) / k <= static_cast<int64_t>(o) * sms) break;
     }
     if (occ <= 0) return nerr(RFMF_ERR_CAPACITY, "no resident launch configuration");
     const int nitems = static_cast<int>((C + K - 1) / K);

@@ -165,29 +165,43 @@ def random_tree(n, signed=False, seed=0, name=None):
 def planar_like(n, avg_degree=11.7, signed=False, seed=0, name=None):
     """Random geometric graph in the unit square with the connection radius
     set for the requested mean degree: spatially local like Gset's planar
-    family G14-G17, G35-G38, G51-G54 (mean degree ~11.7)."""
+    family G14-G17, G35-G38, G51-G54 (mean degree ~11.7).  Edges are every
+    pair within the radius (k-d tree), weights drawn in sorted pair order."""
+    from scipy.spatial import cKDTree
     rng = np.random.default_rng(seed)
     pts = rng.random((n, 2))
     r = math.sqrt(avg_degree / (math.pi * (n - 1)))
-    cell = max(int(1.0 / r), 1)
-    cx = np.minimum((pts[:, 0] * cell).astype(np.int64), cell - 1)
-    cy = np.minimum((pts[:, 1] * cell).astype(np.int64), cell - 1)
-    buckets = {}
-    for i, (a, b) in enumerate(zip(cx, cy)):
-        buckets.setdefault((a, b), []).append(i)
-    us, vs = [], []
-    for (a, b), members in buckets.items():
-        cand = []
-        for da in (-1, 0, 1):
-            for db in (-1, 0, 1):
-                cand.extend(buckets.get((a + da, b + db), []))
-        cand = np.array(cand)
-        for i in members:
-            d = np.sum((pts[cand] - pts[i]) ** 2, axis=1)
-            j = cand[(d <= r * r) & (cand > i)]
-            us.append(np.full(len(j), i))
-            vs.append(j)
-    u = np.concatenate(us)
-    v = np.concatenate(vs)
+    pairs = cKDTree(pts).query_pairs(r, output_type="ndarray")
+    if len(pairs):
+        pairs = pairs[np.lexsort((pairs[:, 1], pairs[:, 0]))]
+    u = pairs[:, 0].astype(np.int64) if len(pairs) else np.zeros(0, np.int64)
+    v = pairs[:, 1].astype(np.int64) if len(pairs) else np.zeros(0, np.int64)
     return csr_from_edges(u, v, _weights(rng, len(u), signed),
                           name=name or f"planar{n}")
+
+
+def erdos_renyi_sparse(n, avg_degree, signed=False, seed=0, name=None):
+    """G(n, p) with p = avg_degree / (n - 1) in O(n + m) time: geometric gaps
+    between successive edges over the row-major upper-triangle pair index
+    (Batagelj and Brandes 2005), for large sparse instances."""
+    rng = np.random.default_rng(seed)
+    p = avg_degree / (n - 1)
+    N = n * (n - 1) // 2
+    ks = []
+    pos = -1
+    while True:
+        need = max(1024, int((N - pos) * p * 1.1) + 64)
+        gaps = rng.geometric(p, size=need)
+        idx = pos + np.cumsum(gaps)
+        ks.append(idx[idx < N])
+        if idx[-1] >= N:
+            break
+        pos = int(idx[-1])
+    k = np.concatenate(ks).astype(np.int64)
+    # row i starts at i*n - i*(i+1)/2 - i ... pair index of (i, j>i)
+    starts = np.arange(n, dtype=np.int64)
+    starts = starts * (2 * n - starts - 1) // 2
+    u = np.searchsorted(starts, k, side="right") - 1
+    v = k - starts[u] + u + 1
+    return csr_from_edges(u, v, _weights(rng, len(u), signed),
+                          name=name or f"er{n}_d{avg_degree}")

@@ -1,0 +1,118 @@
+"""Request server (rfmf_submit / rfmf_poll / rfmf_wait / rfmf_result).
+
+Every request's results must equal a standalone anneal_gpu of the same inputs
+bit for bit (spins, best spins, best and final cuts), whatever shares its
+launch windows: requests on different graphs, schedules, gain widths and
+score paths, admitted at different window boundaries."""
+import threading
+
+import numpy as np
+import pytest
+
+from conftest import chains_for
+
+pytestmark = pytest.mark.gpu
+
+
+def _request(rfmf, g, seeds, t0s, phases, iters):
+    init, solver = chains_for(g, seeds)
+    return dict(g=g, init=init, solver=solver, t0s=t0s, phases=phases, iters=iters)
+
+
+def _standalone(rfmf, ctx, dg, r):
+    return rfmf.anneal_gpu(ctx, dg, r["g"].max_weighted_degree(), r["init"], r["t0s"],
+                           r["phases"], r["iters"], r["solver"])
+
+
+def _same(a, b):
+    assert np.array_equal(a.end_spins, b.end_spins)
+    assert np.array_equal(a.best_spins, b.best_spins)
+    assert np.array_equal(a.best_vals, b.best_vals)
+    assert np.array_equal(a.final_vals, b.final_vals)
+
+
+def test_server_requests_match_standalone(rfmf, ctx):
+    er = rfmf.erdos_renyi(600, 0.03, signed=True, seed=3)
+    tor = rfmf.torus(20, 30, signed=True, seed=4)
+    tree = rfmf.random_tree(900, seed=5)
+    heavy = rfmf.erdos_renyi(300, 0.05, signed=True, seed=6)
+    heavy.weight = heavy.weight * 9            # B > 127: int32 gains
+    reqs = [
+        _request(rfmf, er, list(range(40)), [35.0, 70.0, 140.0, 400.0] * 10,
+                 [128, 16, 2, 1], [300, 300, 300, 300]),
+        _request(rfmf, tor, list(range(100, 124)), [50.0] * 24, [64, 8, 1], [500, 500, 500]),
+        _request(rfmf, tree, list(range(200, 216)), [100.0] * 16, [32, 0, 4], [700, 50, 700]),
+        _request(rfmf, heavy, list(range(300, 310)), [35.0] * 10, [8, 1], [400, 400]),
+        # tiny t0: the int64 score path
+        _request(rfmf, er, list(range(400, 408)), [0.004] * 8, [16, 1], [200, 200]),
+    ]
+    dgs = {}
+    for r in reqs:
+        dgs.setdefault(id(r["g"]), rfmf.DeviceGraph(ctx, r["g"]))
+    srv = rfmf.Server(ctx, window_sweeps=257)
+    ids = []
+    for r in reqs[:3]:
+        ids.append(srv.submit(dgs[id(r["g"])], r["init"], r["t0s"], r["phases"], r["iters"], r["solver"]))
+    srv.wait(ids[0], timeout=120)
+    for r in reqs[3:]:   # join mid-flight
+        ids.append(srv.submit(dgs[id(r["g"])], r["init"], r["t0s"], r["phases"], r["iters"], r["solver"]))
+    for rid, r in zip(ids, reqs):
+        st = srv.wait(rid, timeout=300)
+        assert st["state"] == "done", st
+        assert st["sweeps_done"] == st["sweeps_total"] == sum(i for p, i in zip(r["phases"], r["iters"]) if p)
+        assert st["submit_s"] <= st["start_s"] <= st["finish_s"]
+        _same(srv.result(rid), _standalone(rfmf, ctx, dgs[id(r["g"])], r))
+    stats = srv.stats()
+    assert stats["windows"] >= 6 and stats["launches"] > stats["windows"]   # several launch classes
+    assert stats["queued"] == stats["running"] == stats["done"] == 0
+    srv.close()
+
+
+def test_server_admission_limit_and_threads(rfmf, ctx):
+    g = rfmf.erdos_renyi(400, 0.04, signed=True, seed=8)
+    dg = rfmf.DeviceGraph(ctx, g)
+    srv = rfmf.Server(ctx, window_sweeps=500, max_chains=48)
+    reqs = [_request(rfmf, g, list(range(1000 + 32 * k, 1032 + 32 * k)), [35.0 + k] * 32,
+                     [32, 1], [600, 600]) for k in range(4)]
+    ids = [None] * 4
+
+    def sub(k):
+        r = reqs[k]
+        ids[k] = srv.submit(dg, r["init"], r["t0s"], r["phases"], r["iters"], r["solver"])
+
+    th = [threading.Thread(target=sub, args=(k,)) for k in range(4)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    sts = [srv.wait(rid, timeout=300) for rid in ids]
+    # 48 admitted chains: one 32-chain request at a time
+    spans = sorted((s["start_s"], s["finish_s"]) for s in sts)
+    for (a0, a1), (b0, b1) in zip(spans, spans[1:]):
+        assert b0 >= a1 - 1e-9
+    for rid, r in zip(ids, reqs):
+        _same(srv.result(rid), _standalone(rfmf, ctx, dg, r))
+    srv.close()
+
+
+def test_server_errors(rfmf, ctx):
+    g = rfmf.torus(8, 8, signed=True, seed=1)
+    dg = rfmf.DeviceGraph(ctx, g)
+    srv = rfmf.Server(ctx, window_sweeps=100, max_chains=16)
+    init, solver = chains_for(g, [1, 2])
+    with pytest.raises(rfmf.RfmfError) as ei:
+        srv.submit(dg, init, [35.0, -1.0], [1], [10], solver)
+    assert ei.value.code == 1
+    big, bsolver = chains_for(g, list(range(17)))
+    with pytest.raises(rfmf.RfmfError) as ei:
+        srv.submit(dg, big, [35.0] * 17, [1], [10], bsolver)
+    assert ei.value.code == 4
+    with pytest.raises(rfmf.RfmfError):
+        srv.poll(987654321)
+    rid = srv.submit(dg, init, [35.0, 40.0], [4, 1], [20000, 20000], solver)
+    with pytest.raises(rfmf.RfmfError):
+        srv.result(rid)              # not done yet (40000 sweeps, windows of 100)
+    st = srv.wait(rid, timeout=300)
+    assert st["state"] == "done"
+    srv.result(rid)
+    srv.close()
