@@ -20,6 +20,7 @@
 #ifndef RFMF_H
 #define RFMF_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -112,6 +113,44 @@ void rfmf_initial_spins(uint64_t seed, int64_t n, int8_t* out);
 int rfmf_beta_tables(const double* t0s, int64_t C, int64_t total_steps,
                      int64_t* run_end, int32_t* run_val, int64_t* chain_off,
                      int64_t cap, int64_t* runs);
+
+/* ---- graph ingest -------------------------------------------------------- */
+
+/* Header "N M" of Gset/MQLib text (first line that is neither blank nor a
+ * '#' comment; src/read_gset.cpp:61-75). */
+int rfmf_gset_header(const char* text, size_t len, int64_t* n, int64_t* m);
+
+/*
+ * parseAndScale (src/read_gset.cpp:61-170) on Gset/MQLib text: the M edge
+ * lines "u v w" in file order into u/v/w (cap >= M entries each); when a
+ * weight is fractional the whole instance is scaled by the largest power of
+ * ten (10^-12 .. 10^12) that keeps B and every weight inside the reference's
+ * budgets (forced_scale > 0 overrides), weights are rounded and zeros
+ * dropped.  *nedges = surviving edges, *scale_out the scale, *zero_dropped
+ * the dropped count (both may be NULL).  Not deduplicated.
+ */
+int rfmf_gset_parse(const char* text, size_t len, double forced_scale, int64_t cap,
+                    int64_t* u, int64_t* v, int64_t* w, int64_t* nedges, double* scale_out,
+                    int64_t* zero_dropped);
+
+/*
+ * Graph::addEdge + ImmutableGraph(Graph) (src/graph.cpp, src/immutable_graph.hpp
+ * :44-120) built on the device from an edge list: zero weights are dropped,
+ * an undirected edge seen twice keeps its first weight, the vertices are the
+ * endpoints renumbered densely in ascending original id, each row sorted
+ * ascending.  Ids must lie in [0, 2^28); self loops are refused (the
+ * reference would store them; Gset has none).  *n_out = vertex count (may be
+ * NULL).  The graph is then used exactly like one from rfmf_graph_create.
+ */
+int rfmf_graph_from_edges(rfmf_context* ctx, int64_t nedges, const int64_t* u, const int64_t* v,
+                          const int64_t* w, rfmf_graph** out, int64_t* n_out);
+
+/* Original vertex id of every dense id (graphs from rfmf_graph_from_edges). */
+int rfmf_graph_orig_ids(const rfmf_graph* g, int64_t* out);
+
+/* The graph's CSR copied to the host: offsets[n+1], col/weight[2m] (any may
+ * be NULL). */
+int rfmf_graph_csr(const rfmf_graph* g, uint32_t* offsets, int32_t* col, int32_t* weight);
 
 /* ---- the annealer ------------------------------------------------------ */
 
@@ -209,6 +248,17 @@ typedef struct rfmf_batch_plan {
 int rfmf_batch_info(const rfmf_batch* b, rfmf_batch_plan* out);
 
 int rfmf_batch_destroy(rfmf_batch* b);
+
+/* Output path on the device.  cutValueCsr (src/max_cut.cpp:5-15) of every
+ * chain's end spins (which = 0) or best spins (which = 1), recomputed from
+ * the spins in int64. */
+int rfmf_batch_cuts(rfmf_batch* b, int which, int64_t* out_cuts);
+
+/* Partition strings, the payload of the Solution-*-partition: lines
+ * (src/host_common.cpp:412-422): chain c's n characters '0' (spin -1) /
+ * '1' (spin +1) at out + c * stride (stride >= the largest n; the bytes
+ * past a chain's n are 0). */
+int rfmf_batch_partitions(rfmf_batch* b, int which, char* out, int64_t stride);
 
 /* ---- request server ------------------------------------------------------
  * Serving form of annealGpu (the reference serves one annealGpu call per

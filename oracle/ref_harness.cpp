@@ -87,6 +87,9 @@ void* ref_gset_load(const char* path) {
     return h;
 }
 
+double ref_gset_scale(void* h) { return static_cast<RefGraph*>(h)->stats.scale; }
+int64_t ref_gset_zero_dropped(void* h) { return static_cast<RefGraph*>(h)->stats.zeroDropped; }
+
 int64_t ref_gset_n(void* h) { return static_cast<int64_t>(static_cast<RefGraph*>(h)->csr.numVertices()); }
 int64_t ref_gset_m(void* h) { return static_cast<int64_t>(static_cast<RefGraph*>(h)->csr.numEdges()); }
 

@@ -7,7 +7,8 @@ reference's interface in Python.  There is no CPU fallback.
 from ._lib import BatchPlan, LaunchConfig, RfmfError, lib
 from .api import (SOLVER_SEED_OFFSET, AnnealResult, Batch, Context, DeviceGraph, Server, anneal_gpu,
                   beta_fixed, beta_tables, cut_value, initial_spins, make_config,
-                  max_weighted_degree, score_safe_int32, solver_seed, total_steps, version)
+                  max_weighted_degree, parse_gset, score_safe_int32, solver_seed, total_steps,
+                  version)
 from .graphs import (CsrGraph, csr_from_edges, erdos_renyi, erdos_renyi_degree, erdos_renyi_sparse,
                      planar_like,
                      random_tree, read_gset, torus)
@@ -15,7 +16,7 @@ from .graphs import (CsrGraph, csr_from_edges, erdos_renyi, erdos_renyi_degree, 
 __all__ = [
     "BatchPlan", "LaunchConfig", "RfmfError", "lib", "SOLVER_SEED_OFFSET", "AnnealResult", "Batch",
     "Context", "DeviceGraph", "Server", "anneal_gpu", "beta_fixed", "beta_tables", "cut_value",
-    "initial_spins", "make_config", "max_weighted_degree", "score_safe_int32", "solver_seed",
+    "initial_spins", "make_config", "max_weighted_degree", "parse_gset", "score_safe_int32", "solver_seed",
     "total_steps", "version", "CsrGraph", "csr_from_edges", "erdos_renyi",
     "erdos_renyi_degree", "erdos_renyi_sparse", "planar_like", "random_tree", "read_gset", "torus",
 ]

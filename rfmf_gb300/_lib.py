@@ -46,6 +46,14 @@ SIGNATURES = [
     ("rfmf_batch_destroy", ct.c_int, [_P]),
     ("rfmf_anneal_noalloc", ct.c_int, [ct.c_int, _P, _I64, _P, _P, _I64, _I64, _P, _P, _I64,
                                        _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    ("rfmf_gset_header", ct.c_int, [ct.c_char_p, ct.c_size_t, _P, _P]),
+    ("rfmf_gset_parse", ct.c_int, [ct.c_char_p, ct.c_size_t, ct.c_double, _I64, _P, _P, _P, _P,
+                                   _P, _P]),
+    ("rfmf_graph_from_edges", ct.c_int, [_P, _I64, _P, _P, _P, _P, _P]),
+    ("rfmf_graph_orig_ids", ct.c_int, [_P, _P]),
+    ("rfmf_graph_csr", ct.c_int, [_P, _P, _P, _P]),
+    ("rfmf_batch_cuts", ct.c_int, [_P, ct.c_int, _P]),
+    ("rfmf_batch_partitions", ct.c_int, [_P, ct.c_int, _P, _I64]),
     ("rfmf_server_create", ct.c_int, [_P, _P, _P]),
     ("rfmf_server_destroy", ct.c_int, [_P]),
     ("rfmf_submit", ct.c_int, [_P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P]),

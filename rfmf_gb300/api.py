@@ -31,6 +31,28 @@ def version():
     return lib().rfmf_version().decode()
 
 
+def parse_gset(text, forced_scale=0.0):
+    """Gset/MQLib text (str, bytes or a path) -> dict(n=header N, u, v, w,
+    scale, zero_dropped) with the reference reader's rules (rfmf_gset_parse)."""
+    import os
+    if isinstance(text, (str, os.PathLike)) and os.path.exists(str(text)):
+        with open(text, "rb") as f:
+            data = f.read()
+    else:
+        data = text.encode() if isinstance(text, str) else bytes(text)
+    N, M = ct.c_int64(), ct.c_int64()
+    check(lib().rfmf_gset_header(data, len(data), ct.byref(N), ct.byref(M)))
+    cap = max(M.value, 1)
+    u = np.zeros(cap, np.int64)
+    v = np.zeros(cap, np.int64)
+    w = np.zeros(cap, np.int64)
+    k, scale, dropped = ct.c_int64(), ct.c_double(), ct.c_int64()
+    check(lib().rfmf_gset_parse(data, len(data), float(forced_scale), cap, _p(u), _p(v), _p(w),
+                                ct.byref(k), ct.byref(scale), ct.byref(dropped)))
+    return dict(n=N.value, u=u[:k.value], v=v[:k.value], w=w[:k.value], scale=scale.value,
+                zero_dropped=dropped.value)
+
+
 def initial_spins(seed, n):
     """Chain's initial spins from its RAW seed (src/host_common.cpp:40-45)."""
     out = np.zeros(n, np.int8)
@@ -134,10 +156,43 @@ class DeviceGraph:
         self.g = g
         self.n = g.n
 
+    @classmethod
+    def from_edges(cls, ctx, u, v, w):
+        """Graph built on the device from an edge list (rfmf_graph_from_edges):
+        duplicates keep their first weight, ids renumbered densely in
+        ascending order, rows sorted."""
+        self = cls.__new__(cls)
+        uu = np.ascontiguousarray(u, np.int64)
+        vv = np.ascontiguousarray(v, np.int64)
+        ww = np.ascontiguousarray(w, np.int64)
+        h = ct.c_void_p()
+        n = ct.c_int64()
+        check(lib().rfmf_graph_from_edges(ctx.h, len(uu), _p(uu), _p(vv), _p(ww), ct.byref(h),
+                                          ct.byref(n)))
+        self.h = h
+        self.ctx = ctx
+        self.g = None
+        self.n = n.value
+        return self
+
     def info(self):
         n, m, B = ct.c_int64(), ct.c_int64(), ct.c_int64()
         check(lib().rfmf_graph_info(self.h, ct.byref(n), ct.byref(m), ct.byref(B)))
         return dict(n=n.value, m=m.value, max_weighted_degree=B.value)
+
+    def csr(self):
+        """(offsets, col, weight) copied back from the device."""
+        m = self.info()["m"]
+        off = np.zeros(self.n + 1, np.uint32)
+        col = np.zeros(2 * m, np.int32)
+        w = np.zeros(2 * m, np.int32)
+        check(lib().rfmf_graph_csr(self.h, _p(off), _p(col), _p(w)))
+        return off, col, w
+
+    def orig_ids(self):
+        out = np.zeros(self.n, np.int64)
+        check(lib().rfmf_graph_orig_ids(self.h, _p(out)))
+        return out
 
     def close(self):
         if self.h:
@@ -242,6 +297,20 @@ class Batch:
         splits = np.cumsum(self.ns)[:-1]
         return dict(end_spins=np.split(end, splits), best_spins=np.split(best, splits),
                     cur_vals=cur, best_vals=bv, sweeps_done=done)
+
+    def cuts(self, best=False):
+        """Cut of every chain's end (or best) spins, recomputed on the device."""
+        out = np.zeros(self.C, np.int64)
+        check(lib().rfmf_batch_cuts(self.h, 1 if best else 0, _p(out)))
+        return out
+
+    def partitions(self, best=False):
+        """Partition strings ('0'/'1' per vertex) of every chain, built on the device."""
+        stride = max(self.ns)
+        buf = ct.create_string_buffer(self.C * stride)
+        check(lib().rfmf_batch_partitions(self.h, 1 if best else 0, buf, stride))
+        raw = buf.raw
+        return [raw[c * stride:c * stride + n].decode() for c, n in enumerate(self.ns)]
 
     def best_vals(self):
         """Best cut of every chain so far (waits for launches in flight)."""

@@ -155,12 +155,6 @@ __device__ __forceinline__ int32_t key_vertex(unsigned long long key) {
     return static_cast<int32_t>(~static_cast<uint32_t>(key));
 }
 
-__device__ __forceinline__ unsigned long long shfl_xor_u64(unsigned long long x, int m) {
-    const uint32_t lo = __shfl_xor_sync(0xFFFFFFFFu, static_cast<uint32_t>(x), m);
-    const uint32_t hi = __shfl_xor_sync(0xFFFFFFFFu, static_cast<uint32_t>(x >> 32), m);
-    return (static_cast<unsigned long long>(hi) << 32) | lo;
-}
-
 __device__ __forceinline__ int spin_of(const uint32_t* bits, int v) {
     return (bits[v >> 5] >> (v & 31)) & 1;
 }
@@ -182,6 +176,11 @@ __device__ __forceinline__ void group_sync(int grp, int T) {
 // ------------------------------------------------------------ D storage
 // int32 gains: plain words.
 struct D32 {
+    static constexpr int32_t kBias = 0;
+    // Stored values (D + kBias) of block b; D32 stores D itself.
+    __device__ static __forceinline__ void load8raw(const unsigned char* D, int b, int32_t d[8]) {
+        load8(D, b, d);
+    }
     __device__ static __forceinline__ void load8(const unsigned char* D, int b, int32_t d[8]) {
         const int4 a = *reinterpret_cast<const int4*>(D + 32 * b);
         const int4 c = *reinterpret_cast<const int4*>(D + 32 * b + 16);
@@ -218,7 +217,34 @@ __device__ __forceinline__ int32_t sbyte(uint32_t x) {
     return r;
 }
 
+// Byte k of x zero-extended to 32 bits.
+template <int k>
+__device__ __forceinline__ int32_t ubyte(uint32_t x) {
+    int32_t r;
+    if constexpr (k == 3) {
+        r = static_cast<int32_t>(x >> 24);
+    } else {
+        constexpr uint32_t sel = static_cast<uint32_t>(k) | 0x4440u;
+        asm("prmt.b32 %0, %1, 0, %2;" : "=r"(r) : "r"(x), "n"(sel));
+    }
+    return r;
+}
+
 struct D8 {
+    static constexpr int32_t kBias = 128;
+    // Stored values D + 128 of block b (no sign handling: callers fold the
+    // bias into a constant).
+    __device__ static __forceinline__ void load8raw(const unsigned char* D, int b, int32_t d[8]) {
+        const uint2 w = *reinterpret_cast<const uint2*>(D + 8 * b);
+        d[0] = ubyte<0>(w.x);
+        d[1] = ubyte<1>(w.x);
+        d[2] = ubyte<2>(w.x);
+        d[3] = ubyte<3>(w.x);
+        d[4] = ubyte<0>(w.y);
+        d[5] = ubyte<1>(w.y);
+        d[6] = ubyte<2>(w.y);
+        d[7] = ubyte<3>(w.y);
+    }
     __device__ static __forceinline__ void load8(const unsigned char* D, int b, int32_t d[8]) {
         const uint2 w = *reinterpret_cast<const uint2*>(D + 8 * b);
         const uint32_t a = w.x ^ 0x80808080u, c = w.y ^ 0x80808080u;
@@ -357,10 +383,10 @@ struct PhaseCfg {
     int mode;       // 0: P | 256, groups repeat every P/8 lanes (register fold +
                     //    warp reduction); 1: 8T % P == 0, thread-private groups;
                     // 2: general P, one shared atomic per vertex
-    int period;     // mode 0: lanes sharing a group (P/8, or 1 for P < 8)
-    int jn;         // mode 0: live accumulators after the fold, min(P, 8)
+    int period;     // mode 0: P/8 (or 1 for P < 8); lanes l and l + period share groups
     int g0;         // mode 1: (8 t) mod P
     int laneShift;  // FLIP scatter: log2 of the lanes that share one row
+    uint32_t gmask; // mode 0, P >= 16: the lanes sharing this lane's groups
 };
 
 __device__ __forceinline__ PhaseCfg phase_cfg(int P, int t, int T) {
@@ -368,21 +394,14 @@ __device__ __forceinline__ PhaseCfg phase_cfg(int P, int t, int T) {
     c.P = P;
     c.mode = ((256 % P) == 0) ? 0 : (((8 * T) % P) == 0 ? 1 : 2);
     c.period = (P >= 8) ? (P >> 3) : 1;
-    c.jn = (P < 8) ? P : 8;
     c.g0 = (8 * t) % P;
     int sh = 0;
     while ((2 << sh) * P <= T && sh < 5) ++sh;
     c.laneShift = sh;
+    const uint32_t rep = (c.period >= 32) ? 1u : (c.period == 16) ? 0x00010001u
+                       : (c.period == 8) ? 0x01010101u : (c.period == 4) ? 0x11111111u : 0x55555555u;
+    c.gmask = rep << ((t & 31) & (c.period - 1));
     return c;
-}
-
-// Max of a packed key over the full warp with two redux.sync: the max biased
-// score, then the max ~v (smallest v) among the lanes that hold it.
-__device__ __forceinline__ unsigned long long warp_max_key(unsigned long long k) {
-    const uint32_t hi = static_cast<uint32_t>(k >> 32);
-    const uint32_t mhi = __reduce_max_sync(0xFFFFFFFFu, hi);
-    const uint32_t mlo = __reduce_max_sync(0xFFFFFFFFu, hi == mhi ? static_cast<uint32_t>(k) : 0u);
-    return (static_cast<unsigned long long>(mhi) << 32) | mlo;
 }
 
 // Compact int32 argmax key.  A thread visits its vertex blocks b = t + k*T
@@ -429,28 +448,72 @@ __device__ __forceinline__ KeyCfg key_cfg(int n, int T, int t, const int32_t* lu
     return kc;
 }
 
-__device__ __forceinline__ uint32_t umulhi_add(uint32_t a, uint32_t b, uint32_t c) {
-    uint32_t r;
-    asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
-    return r;
-}
-
 // Keys of one block's 8 vertices folded into acc; lanes j >= lim are skipped
 // (the shuffles still run on every lane: the caller keeps the warp converged).
-template <bool kMasked>
+// `tkb` is this lane's TK[lane & 15] plus the block's constant part
+// (2^kb - 1 - k) - bias * beta * 2^kb, so the shuffle delivers TK[i] with the
+// constant already added and d holds the stored (biased) gains.  All sums are
+// modular int32: only the final key is in range, and it is exact.  kF0: kb ==
+// 4, the field's multiple is the field itself.
+template <bool kMasked, bool kF0>
 __device__ __forceinline__ void score8_key(int32_t acc[8], const uint32_t x[4], const int32_t d[8],
-                                           int32_t betaK, int32_t ck, const KeyCfg& kc, int lim) {
+                                           int32_t betaK, int32_t tkb, const KeyCfg& kc, int lim) {
 #pragma unroll
     for (int w = 0; w < 4; ++w) {
-        const int32_t tk0 = __shfl_sync(0xFFFFFFFFu, kc.tkLane, static_cast<int>(x[w]));
-        const int32_t tk1 = __shfl_sync(0xFFFFFFFFu, kc.tkLane, static_cast<int>(x[w] >> 16));
-        const int32_t f0 = static_cast<int32_t>((x[w] & 0x7FFu) * kc.mulF) + ck;
-        const int32_t f1 = static_cast<int32_t>(
-            umulhi_add(x[w] & 0x07FF0000u, kc.mulHi, static_cast<uint32_t>(ck)));
-        const int32_t k0 = betaK * d[2 * w] + tk0;
-        const int32_t k1 = betaK * d[2 * w + 1] + tk1;
+        const uint32_t xs = x[w] >> 16;
+        const int32_t tk0 = __shfl_sync(0xFFFFFFFFu, tkb, static_cast<int>(x[w]));
+        const int32_t tk1 = __shfl_sync(0xFFFFFFFFu, tkb, static_cast<int>(xs));
+        int32_t f0, f1;
+        if constexpr (kF0) {
+            f0 = static_cast<int32_t>(x[w] & 0x7FFu);
+            f1 = static_cast<int32_t>(xs & 0x7FFu);
+        } else {
+            f0 = static_cast<int32_t>((x[w] & 0x7FFu) * kc.mulF);
+            f1 = static_cast<int32_t>(__umulhi(x[w] & 0x07FF0000u, kc.mulHi));
+        }
+        const int32_t k0 = static_cast<int32_t>(static_cast<uint32_t>(betaK) * static_cast<uint32_t>(d[2 * w]) +
+                                                static_cast<uint32_t>(tk0));
+        const int32_t k1 = static_cast<int32_t>(static_cast<uint32_t>(betaK) * static_cast<uint32_t>(d[2 * w + 1]) +
+                                                static_cast<uint32_t>(tk1));
         if (!kMasked || 2 * w < lim) acc[2 * w] = __viaddmax_s32(k0, f0, acc[2 * w]);
         if (!kMasked || 2 * w + 1 < lim) acc[2 * w + 1] = __viaddmax_s32(k1, f1, acc[2 * w + 1]);
+    }
+}
+
+// NB vertex blocks b, b + T, ... (block iterations k, k + 1, ...) scored with
+// their Philox draws in flight together.
+template <int NB, bool kMasked, bool kF0, class DP>
+__device__ __forceinline__ void score_blocks(int32_t acc[8], const ChainSmem& s, const SweepConst& sc,
+                                             const ChainKeys& keys, int b, int T, int32_t betaK,
+                                             int32_t tkb, const KeyCfg& kc, int lim) {
+    uint32_t x[NB][4];
+    int32_t d[NB][8];
+#pragma unroll
+    for (int q = 0; q < NB; ++q) philox_block(static_cast<uint32_t>(b + q * T), sc, keys, x[q]);
+#pragma unroll
+    for (int q = 0; q < NB; ++q) DP::load8raw(s.D, b + q * T, d[q]);
+#pragma unroll
+    for (int q = 0; q < NB; ++q) score8_key<kMasked, kF0>(acc, x[q], d[q], betaK, tkb - q, kc, lim);
+}
+
+// The block loop of select32 (trip counts uniform per warp: its blocks at
+// step k are wb + kT .. wb + kT + 31, so the table shuffles run converged):
+// two blocks in flight while the whole warp has two full blocks left, then a
+// clamped, masked single-block tail.
+template <bool kF0, class DP>
+__device__ __forceinline__ void select_blocks(int32_t acc[8], const ChainSmem& s, const SweepConst& sc,
+                                              const ChainKeys& keys, int n, int t, int T,
+                                              int32_t betaK, int32_t tkBase, const KeyCfg& kc) {
+    const int nfull = n >> 3;
+    const int nblk = (n + 7) >> 3;
+    const int wb = t & ~31;
+    int b = t, k = 0;
+    for (; wb + T + 31 < nfull - k * T; b += 2 * T, k += 2)
+        score_blocks<2, false, kF0, DP>(acc, s, sc, keys, b, T, betaK, tkBase - k, kc, 8);
+    for (; wb + k * T < nblk; b += T, ++k) {
+        const int bb = (b < nblk) ? b : nblk - 1;
+        const int lim = (b < nfull) ? 8 : ((b == nfull) ? (n & 7) : 0);
+        score_blocks<1, true, kF0, DP>(acc, s, sc, keys, bb, T, betaK, tkBase - k, kc, lim);
     }
 }
 
@@ -459,8 +522,6 @@ __device__ void select32(const ChainSmem& s, const int32_t* lut, const KeyCfg& k
                          const PhaseCfg& pc, int32_t beta, uint64_t step, const ChainKeys& keys,
                          int t, int T) {
     const SweepConst sc = make_sweep(step, keys);
-    const int nfull = n >> 3;
-    const int nblk = (n + 7) >> 3;
     const int P = pc.P;
     const int M = (1 << kc.kb) - 1;
     if (pc.mode != 2) {
@@ -468,77 +529,83 @@ __device__ void select32(const ChainSmem& s, const int32_t* lut, const KeyCfg& k
         int32_t acc[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) acc[j] = INT32_MIN;
-        // Trip counts are uniform over each warp (its blocks at step k are
-        // wb + kT .. wb + kT + 31), so the table shuffles run converged.
+        // Per-sweep part of the table register: (2^kb - 1) - bias * beta * 2^kb.
+        const int32_t tkBase = static_cast<int32_t>(static_cast<uint32_t>(kc.tkLane) + static_cast<uint32_t>(M) -
+                                                    static_cast<uint32_t>(DP::kBias) * static_cast<uint32_t>(betaK));
+        if (kc.kb == 4) select_blocks<true, DP>(acc, s, sc, keys, n, t, T, betaK, tkBase, kc);
+        else select_blocks<false, DP>(acc, s, sc, keys, n, t, T, betaK, tkBase, kc);
         const int wb = t & ~31;
-        int b = t, k = 0;
-        for (; wb + T + 31 < nfull - k * T; b += 2 * T, k += 2) {
-            uint32_t xa[4], xb[4];
-            int32_t da[8], db[8];
-            philox_block(static_cast<uint32_t>(b), sc, keys, xa);
-            philox_block(static_cast<uint32_t>(b + T), sc, keys, xb);
-            DP::load8(s.D, b, da);
-            DP::load8(s.D, b + T, db);
-            score8_key<false>(acc, xa, da, betaK, M - k, kc, 8);
-            score8_key<false>(acc, xb, db, betaK, M - k - 1, kc, 8);
-        }
-        for (; wb + k * T < nblk; b += T, ++k) {
-            // Tail: blocks past the last one are clamped and masked out.
-            const int bb = (b < nblk) ? b : nblk - 1;
-            const int lim = (b < nfull) ? 8 : ((b == nfull) ? (n & 7) : 0);
-            uint32_t xa[4];
-            int32_t da[8];
-            philox_block(static_cast<uint32_t>(bb), sc, keys, xa);
-            DP::load8(s.D, bb, da);
-            score8_key<true>(acc, xa, da, betaK, M - k, kc, lim);
-        }
-        // Back to (score, v) as a packed 64-bit key for the group reduction.
-        unsigned long long key[8];
+        // Group argmax on the compact keys.  Equal keys mean equal score and
+        // block iteration k, so they differ only in the thread t (vertex
+        // 8(t + kT) + j): the lowest lane holding the maximum wins.  Only the
+        // winners are widened to packed (score, v) keys for the slots.
+        const int lane = t & 31;
+        if (pc.mode == 0 && P <= 8) {
+            int32_t mj[8];
+            int32_t vj[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int kk = M - (acc[j] & M);
-            const int v = 8 * (t + kk * T) + j;
-            key[j] = (acc[j] == INT32_MIN) ? 0ull : pack_key(acc[j] >> kc.kb, v);
-        }
-        if (pc.mode == 0) {
-            // Groups repeat every P/8 lanes inside a warp's 256 vertices:
-            // fold accumulators (P < 8) and lanes that share a group.
+            for (int j = 0; j < 8; ++j) {
+                mj[j] = __reduce_max_sync(0xFFFFFFFFu, acc[j]);
+                const uint32_t bal = __ballot_sync(0xFFFFFFFFu, acc[j] == mj[j]);
+                const int kk = M - (mj[j] & M);
+                vj[j] = 8 * (wb + (__ffs(bal) - 1) + kk * T) + j;
+            }
+            // Groups g < P collect j = g, g + P, ...: larger key, then smaller v.
             if (P <= 4) {
 #pragma unroll
-                for (int j = 0; j < 4; ++j) if (key[j + 4] > key[j]) key[j] = key[j + 4];
+                for (int j = 0; j < 4; ++j)
+                    if (mj[j + 4] > mj[j] || (mj[j + 4] == mj[j] && vj[j + 4] < vj[j])) {
+                        mj[j] = mj[j + 4];
+                        vj[j] = vj[j + 4];
+                    }
             }
             if (P <= 2) {
 #pragma unroll
-                for (int j = 0; j < 2; ++j) if (key[j + 2] > key[j]) key[j] = key[j + 2];
-            }
-            if (P == 1) {
-                if (key[1] > key[0]) key[0] = key[1];
-            }
-            if (P <= 8) {
-#pragma unroll
-                for (int j = 0; j < 8; ++j)
-                    if (j < pc.jn) key[j] = warp_max_key(key[j]);
-            } else {
-#pragma unroll
-                for (int m = 16; m >= 2; m >>= 1) {
-                    if (m >= pc.period) {
-#pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            const unsigned long long o = shfl_xor_u64(key[j], m);
-                            if (o > key[j]) key[j] = o;
-                        }
+                for (int j = 0; j < 2; ++j)
+                    if (mj[j + 2] > mj[j] || (mj[j + 2] == mj[j] && vj[j + 2] < vj[j])) {
+                        mj[j] = mj[j + 2];
+                        vj[j] = vj[j + 2];
                     }
+            }
+            if (P == 1 && (mj[1] > mj[0] || (mj[1] == mj[0] && vj[1] < vj[0]))) {
+                mj[0] = mj[1];
+                vj[0] = vj[1];
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                if (lane == j && j < P && mj[j] != INT32_MIN) {
+                    const unsigned long long key = pack_key(mj[j] >> kc.kb, vj[j]);
+                    if (T == 32) s.slots[j] = key;
+                    else atomicMax(&s.slots[j], key);
                 }
             }
-            const int lane = t & 31;
+        } else if (pc.mode == 0) {
+            // P = 8p, p = P/8 in {2..32}: lanes r, r + p, ... share group 8r + j.
+            // Shuffle steps outermost so the eight chains overlap, then one
+            // divergent block for the p writing lanes.
+            int32_t mx[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) mx[j] = acc[j];
+#pragma unroll
+            for (int m = 16; m >= 2; m >>= 1) {
+                if (m >= pc.period) {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) mx[j] = max(mx[j], __shfl_xor_sync(0xFFFFFFFFu, mx[j], m));
+                }
+            }
+            uint32_t bal[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) bal[j] = __ballot_sync(0xFFFFFFFFu, acc[j] == mx[j]) & pc.gmask;
             if (lane < pc.period) {
-                // lane < P/8 (or lane 0): group 8*lane + j (or j) is < P.
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
-                    if (j < pc.jn && key[j]) {
+                    if (mx[j] != INT32_MIN) {
+                        const int kk = M - (mx[j] & M);
+                        const int v = 8 * (wb + (__ffs(bal[j]) - 1) + kk * T) + j;
+                        const unsigned long long key = pack_key(mx[j] >> kc.kb, v);
                         const int g = 8 * lane + j;
-                        if (T == 32) s.slots[g] = key[j];
-                        else atomicMax(&s.slots[g], key[j]);
+                        if (T == 32) s.slots[g] = key;
+                        else atomicMax(&s.slots[g], key);
                     }
                 }
             }
@@ -546,7 +613,10 @@ __device__ void select32(const ChainSmem& s, const int32_t* lut, const KeyCfg& k
             int g = pc.g0;
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                if (key[j]) atomicMax(&s.slots[g], key[j]);
+                if (acc[j] != INT32_MIN) {
+                    const int kk = M - (acc[j] & M);
+                    atomicMax(&s.slots[g], pack_key(acc[j] >> kc.kb, 8 * (t + kk * T) + j));
+                }
                 if (++g == P) g = 0;
             }
         }

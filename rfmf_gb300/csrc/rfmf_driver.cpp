@@ -1032,6 +1032,40 @@ extern "C" int rfmf_batch_read(rfmf_batch* b, int8_t* end_spins, int8_t* best_sp
     return RFMF_OK;
 }
 
+extern "C" int rfmf_batch_cuts(rfmf_batch* b, int which, int64_t* out_cuts) {
+    if (!b || !out_cuts || (which != 0 && which != 1)) return fail(RFMF_ERR_INVALID, "bad arguments");
+    if (int rc = rfmf_batch_synchronize(b)) return rc;
+    DevBuf d;
+    if (int rc = d.alloc(b->C * sizeof(int64_t))) return rc;
+    CU(launch_chain_cuts(b->L.chains, b->L.graphs, static_cast<int>(b->C), which, d.as<int64_t>(),
+                         b->ctx->stream));
+    CU(cudaMemcpyAsync(out_cuts, d.p, b->C * sizeof(int64_t), cudaMemcpyDeviceToHost, b->ctx->stream));
+    CU(cudaStreamSynchronize(b->ctx->stream));
+    return RFMF_OK;
+}
+
+extern "C" int rfmf_batch_partitions(rfmf_batch* b, int which, char* out, int64_t stride) {
+    if (!b || !out || (which != 0 && which != 1)) return fail(RFMF_ERR_INVALID, "bad arguments");
+    int64_t maxN = 0;
+    for (int64_t n : b->chainN) maxN = std::max(maxN, n);
+    if (stride < maxN) return fail(RFMF_ERR_INVALID, "stride %lld < largest n %lld", (long long)stride, (long long)maxN);
+    if (int rc = rfmf_batch_synchronize(b)) return rc;
+    // chunks of chains bounded to ~256 MB of device staging
+    const int64_t per = std::max<int64_t>(1, std::min<int64_t>(b->C, (int64_t(256) << 20) / std::max<int64_t>(stride, 1)));
+    DevBuf d;
+    if (int rc = d.alloc(static_cast<size_t>(per * stride))) return rc;
+    for (int64_t c0 = 0; c0 < b->C; c0 += per) {
+        const int64_t cnt = std::min(per, b->C - c0);
+        CU(cudaMemsetAsync(d.p, 0, static_cast<size_t>(cnt * stride), b->ctx->stream));
+        CU(launch_chain_partitions(b->L.chains, b->L.graphs, static_cast<int>(c0), static_cast<int>(cnt),
+                                   static_cast<int>(maxN), which, d.as<char>(), stride, b->ctx->stream));
+        CU(cudaMemcpyAsync(out + c0 * stride, d.p, static_cast<size_t>(cnt * stride), cudaMemcpyDeviceToHost,
+                           b->ctx->stream));
+        CU(cudaStreamSynchronize(b->ctx->stream));
+    }
+    return RFMF_OK;
+}
+
 extern "C" int rfmf_batch_info(const rfmf_batch* b, rfmf_batch_plan* out) {
     if (!b || !out) return fail(RFMF_ERR_INVALID, "batch/out is NULL");
     out->nchains = b->C;

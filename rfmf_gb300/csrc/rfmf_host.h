@@ -20,6 +20,12 @@ const void* kernel_ptr(int dbytes, int fmt, bool s64);
 cudaError_t launch_anneal(const DevLaunch& L, int dbytes, int fmt, bool s64, int grid,
                           int threads, size_t smem, cudaStream_t stream);
 
+// Output-path kernels (rfmf_ingest.cu).
+cudaError_t launch_chain_cuts(const DevChain* chains, const DevGraph* graphs, int C, int which,
+                              int64_t* out, cudaStream_t st);
+cudaError_t launch_chain_partitions(const DevChain* chains, const DevGraph* graphs, int c0, int count,
+                                    int maxN, int which, char* out, int64_t stride, cudaStream_t st);
+
 // Error channel: records the message for rfmf_last_error() (per host thread)
 // and returns `code`.
 int fail(int code, const char* fmt, ...);
@@ -100,6 +106,8 @@ struct rfmf_graph {
     // timings of earlier launches (weight = chain-sweeps observed).  Feeds the
     // work-item sizing of later launches; never affects results.
     mutable double costNs = 0.0, costWeight = 0.0;
+    // Original vertex ids by dense id (graphs built from an edge list).
+    std::vector<int64_t> origIds;
 };
 
 #endif  // RFMF_HOST_H
