@@ -254,6 +254,7 @@ def gpu_arm(args, rank, world):
         dist.barrier()
     torch.cuda.synchronize()
     clocks.start()
+    time.sleep(1.0)   # let the sampler's first NVML queries finish before the timed region
     t_wall = time.perf_counter()
     step_ms, step_bytes, best_by_step = [], [], []
     imp_prev = np.zeros(len(graphs) * args.chains, np.uint64)
