@@ -243,6 +243,7 @@ typedef struct rfmf_batch_plan {
     int gain_width;            /* bytes per vertex gain: 1 or 4 */
     int smem_bytes;            /* dynamic shared memory per CTA */
     int balanced;              /* 1 once work items are sized from learned graph costs */
+    int launch_classes;        /* launches per window (graphs grouped by kernel variant and size) */
 } rfmf_batch_plan;
 
 int rfmf_batch_info(const rfmf_batch* b, rfmf_batch_plan* out);

@@ -19,8 +19,8 @@ INCLUDE = PKG.parent / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-Wall", "-I", str(INCLUDE), "-I", str(CSRC)]
-SOURCES = ["rfmf_anneal.cu", "rfmf_driver.cpp", "rfmf_noalloc.cu", "rfmf_server.cpp",
-           "rfmf_ingest.cu"]
+SOURCES = ["rfmf_anneal.cu", "rfmf_driver.cpp", "rfmf_batch.cpp", "rfmf_noalloc.cu",
+           "rfmf_server.cpp", "rfmf_ingest.cu"]
 
 
 def nvcc():

@@ -517,10 +517,31 @@ __device__ __forceinline__ void select_blocks(int32_t acc[8], const ChainSmem& s
     }
 }
 
-template <class DP>
-__device__ void select32(const ChainSmem& s, const int32_t* lut, const KeyCfg& kc, int n,
+// FLIP step 1 for one winner v (or none, v < 0) of group g: publish it, add
+// its pre-sweep gain to loc, negate the gain, flip the spin bit and byte.
+template <class DP, class Loc>
+__device__ __forceinline__ void flip_winner(const ChainSmem& s, int g, int v, Loc& loc) {
+    s.win[g] = v;
+    if (v >= 0) {
+        const int32_t d = DP::get(s.D, v);
+        loc += d;
+        DP::set(s.D, v, -d);
+        atomicXor(&s.bits[v >> 5], 1u << (v & 31));
+        s.sb[v] ^= 1u;
+    }
+}
+
+// How select32 hands its winners to FLIP step 1.
+enum WinnerHandoff : int {
+    kWinSlots = 0,      // packed keys in the group slots (any warp count, any P)
+    kWinFlipped = 1,    // FLIP step 1 done here (one-warp chains, P <= 8)
+    kWinPublished = 2   // winner ids in s.win (one-warp chains, P >= 16)
+};
+
+template <class DP, class Loc>
+__device__ int select32(const ChainSmem& s, const int32_t* lut, const KeyCfg& kc, int n,
                          const PhaseCfg& pc, int32_t beta, uint64_t step, const ChainKeys& keys,
-                         int t, int T) {
+                         int t, int T, Loc& loc) {
     const SweepConst sc = make_sweep(step, keys);
     const int P = pc.P;
     const int M = (1 << kc.kb) - 1;
@@ -571,13 +592,19 @@ __device__ void select32(const ChainSmem& s, const int32_t* lut, const KeyCfg& k
                 mj[0] = mj[1];
                 vj[0] = vj[1];
             }
+            if (T == 32) {
+                // Every lane holds every group's winner: lane g flips group g.
+                int mine = -1;
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    if (lane == j) mine = (mj[j] != INT32_MIN) ? vj[j] : -1;
+                if (lane < P) flip_winner<DP>(s, lane, mine, loc);
+                return kWinFlipped;
+            }
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                if (lane == j && j < P && mj[j] != INT32_MIN) {
-                    const unsigned long long key = pack_key(mj[j] >> kc.kb, vj[j]);
-                    if (T == 32) s.slots[j] = key;
-                    else atomicMax(&s.slots[j], key);
-                }
+                if (lane == j && j < P && mj[j] != INT32_MIN)
+                    atomicMax(&s.slots[j], pack_key(mj[j] >> kc.kb, vj[j]));
             }
         } else if (pc.mode == 0) {
             // P = 8p, p = P/8 in {2..32}: lanes r, r + p, ... share group 8r + j.
@@ -599,16 +626,14 @@ __device__ void select32(const ChainSmem& s, const int32_t* lut, const KeyCfg& k
             if (lane < pc.period) {
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
-                    if (mx[j] != INT32_MIN) {
-                        const int kk = M - (mx[j] & M);
-                        const int v = 8 * (wb + (__ffs(bal[j]) - 1) + kk * T) + j;
-                        const unsigned long long key = pack_key(mx[j] >> kc.kb, v);
-                        const int g = 8 * lane + j;
-                        if (T == 32) s.slots[g] = key;
-                        else atomicMax(&s.slots[g], key);
-                    }
+                    const int kk = M - (mx[j] & M);
+                    const int v = 8 * (wb + (__ffs(bal[j]) - 1) + kk * T) + j;
+                    const int g = 8 * lane + j;
+                    if (T == 32) s.win[g] = (mx[j] != INT32_MIN) ? v : -1;
+                    else if (mx[j] != INT32_MIN) atomicMax(&s.slots[g], pack_key(mx[j] >> kc.kb, v));
                 }
             }
+            if (T == 32) return kWinPublished;
         } else {
             int g = pc.g0;
 #pragma unroll
@@ -640,6 +665,7 @@ __device__ void select32(const ChainSmem& s, const int32_t* lut, const KeyCfg& k
             }
         }
     }
+    return kWinSlots;
 }
 
 // int64 scores (the reference's two-pass path, src/anneal_kernels.cu:348-378,
@@ -720,11 +746,40 @@ __device__ void select64(const ChainSmem& s, const int32_t* lut, int n, const Ph
 }
 
 // ------------------------------------------------------------------ chain
+// Pacing between the chains of one CTA.  The warp scheduler does not share
+// issue slots evenly, so chains of one item drift apart within a window (by
+// up to ~40% of it measured on GB300), and the CTA then runs its last chains
+// with few warps while the others wait at the item barrier.  Every
+// kPaceEvery sweeps a chain publishes its progress; one more than kPaceLead
+// sweeps ahead of the slowest chain of its CTA yields its issue slots with
+// short sleeps (bounded: at most kPaceSleeps of them per check).
+constexpr int kPaceEvery = 32;
+constexpr int kPaceLead = 64;
+constexpr int kPaceSleeps = 32;
+
+// The CTA header holds the pacing state: progress of each warp group at
+// bytes 160..223, the number of running groups at 224.
+__device__ __forceinline__ volatile int* pace_state() {
+    extern __shared__ __align__(128) unsigned char smem[];
+    return reinterpret_cast<volatile int*>(smem + 160);
+}
+
+__device__ __forceinline__ int slowest_chain(const volatile int* prog) {
+    const int active = prog[16];
+    int m = INT_MAX;
+    for (int q = 0; q < active; ++q) m = min(m, prog[q]);
+    return m;
+}
+
 template <class DP, int kFmt, bool kS64>
 __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView& csr,
                           const int32_t* lut, int ci, int t, int T, int grp) {
+    volatile int* prog = pace_state();
     DevChain& ch = L.chains[ci];
-    if (ch.sweepsDone >= ch.sweepsTotal && ch.cur != kUnsetCut) return;
+    if (ch.sweepsDone >= ch.sweepsTotal && ch.cur != kUnsetCut) {
+        if (t == 0) prog[grp] = INT_MAX;
+        return;
+    }
     const DevGraph& g = L.graphs[ch.graph];
     const DevSchedule sch = L.scheds[ch.sched];
     const int n = g.n;
@@ -789,7 +844,10 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
     }
     if (s1 > s0 && (run >= ch.betaRuns ||
                     static_cast<uint64_t>(ch.betaEnd[ch.betaRuns - 1]) < s1)) {
-        if (t == 0) raise_error(L, kDevBetaTable, ci);
+        if (t == 0) {
+            raise_error(L, kDevBetaTable, ci);
+            prog[grp] = INT_MAX;
+        }
         return;
     }
     int p = 0;
@@ -847,34 +905,41 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
                 pfVal = __ldg(bVal + run + 1);
             }
         }
+        if (((sw - s0) & (kPaceEvery - 1)) == 0) {
+            const int mine = static_cast<int>(sw - s0);
+            if (t == 0) prog[grp] = mine;
+            int lead = mine - slowest_chain(prog);
+            for (int q = 0; q < kPaceSleeps && lead > kPaceLead; ++q) {
+                __nanosleep(2000);
+                lead = mine - slowest_chain(prog);
+            }
+        }
         const uint64_t step = sw + 1;   // 1-based sweep id
 
-        if constexpr (kS64) select64<DP>(s, lut, n, pc, beta, step, keys, t, T, grp);
-        else select32<DP>(s, lut, kc, n, pc, beta, step, keys, t, T);
-        group_sync(grp, T);
-
-        // ---- FLIP 1: winners; negate their gains, flip their spins
         using Loc = typename std::conditional<std::is_same<DP, D8>::value, int32_t, int64_t>::type;
         Loc loc = 0;
-        for (int gi = t; gi < P; gi += T) {
-            int v;
-            if constexpr (kS64) {
-                const int32_t id = s.ids[gi];
-                v = (id == INT32_MAX) ? -1 : id;
-                s.scores[gi] = LLONG_MIN;
-                s.ids[gi] = INT32_MAX;
-            } else {
-                const unsigned long long k = s.slots[gi];
-                s.slots[gi] = 0ull;
-                v = k ? key_vertex(k) : -1;
-            }
-            s.win[gi] = v;
-            if (v >= 0) {
-                const int32_t d = DP::get(s.D, v);
-                loc += d;
-                DP::set(s.D, v, -d);
-                atomicXor(&s.bits[v >> 5], 1u << (v & 31));
-                s.sb[v] ^= 1u;
+        int handoff = kWinSlots;
+        if constexpr (kS64) select64<DP>(s, lut, n, pc, beta, step, keys, t, T, grp);
+        else handoff = select32<DP>(s, lut, kc, n, pc, beta, step, keys, t, T, loc);
+
+        // ---- FLIP 1: winners; negate their gains, flip their spins
+        if (handoff != kWinFlipped) {
+            group_sync(grp, T);
+            for (int gi = t; gi < P; gi += T) {
+                int v;
+                if constexpr (kS64) {
+                    const int32_t id = s.ids[gi];
+                    v = (id == INT32_MAX) ? -1 : id;
+                    s.scores[gi] = LLONG_MIN;
+                    s.ids[gi] = INT32_MAX;
+                } else if (handoff == kWinPublished) {
+                    v = s.win[gi];
+                } else {
+                    const unsigned long long k = s.slots[gi];
+                    s.slots[gi] = 0ull;
+                    v = k ? key_vertex(k) : -1;
+                }
+                flip_winner<DP>(s, gi, v, loc);
             }
         }
         group_sync(grp, T);
@@ -928,6 +993,7 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
             for (int w = t; w < words; w += T) s.best[w] = s.bits[w];
         }
     }
+    if (t == 0) prog[grp] = INT_MAX;
     group_sync(grp, T);
 
     // ---- state out
@@ -1012,6 +1078,7 @@ __global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) 
     int32_t* lut = reinterpret_cast<int32_t*>(smem);                 // 64 B
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + 128);        // 8 B
     int* sItem = reinterpret_cast<int*>(smem + 144);
+    volatile int* sProg = pace_state();   // 16 progress words + running-group count
     unsigned char* csrBase = smem + kSmemHeader;
     unsigned char* chainBase = csrBase + L.csrBytes;
 
@@ -1058,8 +1125,11 @@ __global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) 
             csr.off = reinterpret_cast<const uint32_t*>(csrBase);
             csr.ent = csrBase + g.offBytes;
         }
+        const int active = (item.count < L.chainsPerCta) ? item.count : L.chainsPerCta;
+        if (threadIdx.x < 16) sProg[threadIdx.x] = (static_cast<int>(threadIdx.x) < active) ? 0 : INT_MAX;
+        if (threadIdx.x == 0) sProg[16] = active;
         __syncthreads();
-        if (!dead && grp < item.count && grp < L.chainsPerCta)
+        if (!dead && grp < active)
             run_chain<DP, kFmt, kS64>(L, cs, csr, lut, L.order[item.first + grp], t, T, grp);
         __syncthreads();
         if (threadIdx.x == 0 && L.itemNs) {

@@ -116,7 +116,7 @@ struct DevLaunch {
 constexpr int64_t kUnsetCut = INT64_MIN;
 
 // Shared-memory header in front of the CSR region: Gumbel table (64 B),
-// bulk-copy mbarrier, work-item slot.
+// bulk-copy mbarrier, work-item slot, chain pacing state (bytes 160..227).
 constexpr uint32_t kSmemHeader = 256;
 
 #if defined(__CUDACC__)

@@ -165,36 +165,6 @@ bool score_safe_int32(int64_t total, double t0, int64_t B) {
 
 }  // namespace rfmf
 
-struct rfmf_batch {
-    rfmf_context* ctx = nullptr;
-    int64_t C = 0;
-    uint64_t total = 0;
-    bool score64 = false;
-    int dbytes = 4, fmt = kCsrGlobal, warps = 1, K = 1, threads = 32, grid = 0, pmax = 0;
-    int nitems = 0;
-    size_t smem = 0;
-    std::vector<int64_t> chainN, chainWordOff;   // per chain
-    std::vector<int64_t> graphOfChain;
-    int64_t words = 0;                           // total spin words over chains
-    DevBuf dGraphs, dScheds, dChains, dItems, dOrder, dPhaseP, dPhaseIters, dBetaEnd, dBetaVal,
-        dBits, dBest, dCtl, dItemNs;
-    DevLaunch L{};
-    // Work-item state: graphs, their chains, current per-graph chains per item.
-    std::vector<const rfmf_graph*> glist;
-    std::vector<std::vector<int32_t>> chainsOf;
-    std::vector<int> Kg;
-    std::vector<DevItem> items;
-    std::vector<int32_t> order;
-    int occ = 1;                 // resident CTAs per SM for the launch shape
-    bool balanced = false;       // items sized from learned graph costs
-    uint64_t hostDone = 0;       // sweeps every chain has been advanced by
-    uint64_t pendingSweeps = 0;  // sweeps of launches whose item times are unread
-    cudaGraphExec_t graphExec = nullptr;
-    uint64_t graphSweeps = 0;
-    int graphLaunches = 0;
-    ~rfmf_batch() { if (graphExec) cudaGraphExecDestroy(graphExec); }
-};
-
 // Error channel shared with the other translation units of the library.
 namespace rfmf {
 int set_last_error(int code, const char* msg) { return fail(code, "%s", msg); }
@@ -482,674 +452,4 @@ bool compact_key_safe(int64_t total, double t0, int64_t B, int kb) {
 }
 
 }  // namespace rfmf
-
-namespace {
-
-// Launch plan: gain width, CSR format, warps per chain W, chains per CTA K.
-//  * gain width: int8 when every graph has B <= 127, else int32;
-//  * CSR format: the most compact shared-memory format every graph supports
-//    (unit16, else packed32), else HBM walks;
-//  * W: one warp per chain unless a chain has enough vertex blocks to keep
-//    more warps busy (about 384 blocks of 8 vertices per extra warp);
-//  * K: the smallest number of chains per CTA that lets every work item be
-//    resident at once (one wave), within shared memory, the kernel's CTA
-//    thread limit and the named-barrier budget; with more chains than that,
-//    the largest.
-struct Plan {
-    int dbytes, fmt, warps, K, Kuniform, threads, grid, nitems, pmax, occ;
-    uint32_t csrBytes, chainBytes;
-    size_t smem;
-};
-
-int plan_launch(rfmf_batch& b, const std::vector<const rfmf_graph*>& glist,
-                const std::vector<int64_t>& perGraphChains, int maxN, int maxWords,
-                int64_t maxB, const rfmf_launch_config& c, Plan& pl) {
-    const int sms = b.ctx->sms;
-    pl.pmax = b.pmax;
-    // gain width
-    pl.dbytes = c.gain_width ? c.gain_width : (maxB <= 127 ? 1 : 4);
-    if (pl.dbytes != 1 && pl.dbytes != 4) return fail(RFMF_ERR_INVALID, "gain_width must be 0, 1 or 4");
-    if (pl.dbytes == 1 && maxB > 127)
-        return fail(RFMF_ERR_INVALID, "int8 gains need max weighted degree <= 127 (B=%lld)", (long long)maxB);
-    // CSR format
-    bool allU16 = true, allP32 = true;
-    for (const rfmf_graph* g : glist) { allU16 = allU16 && g->unit16; allP32 = allP32 && g->packed32; }
-    int fmt;
-    if (c.csr_format == 0) fmt = allU16 ? kCsrUnit16 : (allP32 ? kCsrPacked32 : kCsrGlobal);
-    else if (c.csr_format == 1) { if (!allU16) return fail(RFMF_ERR_INVALID, "unit16 CSR needs |w| == 1 and n <= 32768"); fmt = kCsrUnit16; }
-    else if (c.csr_format == 2) { if (!allP32) return fail(RFMF_ERR_INVALID, "packed32 CSR needs |w| < 2^15 and n <= 65536"); fmt = kCsrPacked32; }
-    else if (c.csr_format == 3) fmt = kCsrGlobal;
-    else return fail(RFMF_ERR_INVALID, "csr_format must be 0..3");
-    // warps per chain
-    const int W = choose_warps(maxN, c);
-    const void* kern = kernel_ptr(pl.dbytes, kCsrGlobal, b.score64);
-    cudaFuncAttributes fa{};
-    CU(cudaFuncGetAttributes(&fa, kern));
-    const int64_t dynMax = static_cast<int64_t>(b.ctx->smemOptin) - static_cast<int64_t>(fa.sharedSizeBytes);
-    for (int attempt = 0; attempt < 2; ++attempt) {
-        uint32_t csrBytes = 0;
-        if (fmt != kCsrGlobal)
-            for (const rfmf_graph* g : glist)
-                csrBytes = std::max(csrBytes, g->offBytes + (fmt == kCsrUnit16 ? g->u16Bytes : g->p32Bytes));
-        const uint32_t chainBytes = chain_layout(maxN, maxWords, pl.pmax, W, pl.dbytes).total;
-        const void* k2 = kernel_ptr(pl.dbytes, fmt, b.score64);
-        cudaFuncAttributes fa2{};
-        CU(cudaFuncGetAttributes(&fa2, k2));
-        // Warp groups per CTA: named barriers 1..15, and the variant's
-        // register budget bounds the CTA's threads.
-        const int kCap = std::min(std::min(16 / W, W > 1 ? 15 : 16), fa2.maxThreadsPerBlock / (32 * W));
-        if (kCap < 1) return fail(RFMF_ERR_CAPACITY, "a %d-thread chain exceeds the kernel's CTA limit", 32 * W);
-        const int64_t room = dynMax - kSmemHeader - csrBytes;
-        int Kmax = room > 0 ? static_cast<int>(std::min<int64_t>(kCap, room / chainBytes)) : 0;
-        if (c.chains_per_cta) {
-            if (c.chains_per_cta < 1 || c.chains_per_cta > kCap)
-                return fail(RFMF_ERR_INVALID, "chains_per_cta must be 0 or 1..%d", kCap);
-            Kmax = std::min(Kmax, c.chains_per_cta);
-        }
-        if (Kmax < 1) {
-            if (fmt != kCsrGlobal && c.csr_format == 0) { fmt = kCsrGlobal; continue; }
-            return fail(RFMF_ERR_CAPACITY,
-                        "one chain needs %u B of shared memory beside a %u B CSR, but a CTA "
-                        "has %lld B", chainBytes, csrBytes, static_cast<long long>(dynMax));
-        }
-        CU(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dynMax)));
-        CU(cudaFuncSetAttribute(k2, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                cudaSharedmemCarveoutMaxShared));
-        auto items_for = [&](int K) {
-            int64_t it = 0;
-            for (int64_t cg : perGraphChains) it += (cg + K - 1) / K;
-            return it;
-        };
-        // CTA shape: Kmax warp groups (headroom for uneven per-graph items);
-        // the first launch uses the smallest uniform K that fits one wave.
-        int occ = 0;
-        int Kshape = Kmax;
-        for (; Kshape >= 1; --Kshape) {
-            const size_t smem = kSmemHeader + csrBytes + static_cast<size_t>(Kshape) * chainBytes;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k2, 32 * W * Kshape, smem) !=
-                cudaSuccess) {
-                cudaGetLastError();
-                occ = 0;
-            }
-            if (occ > 0) break;
-        }
-        if (Kshape < 1 || occ <= 0)
-            return fail(RFMF_ERR_CAPACITY, "no resident configuration for %u B CSR + %u B per chain",
-                        csrBytes, chainBytes);
-        const int64_t slots = static_cast<int64_t>(occ) * sms;
-        int Kuni = c.chains_per_cta ? Kshape : 1;
-        while (Kuni < Kshape && items_for(Kuni) > slots) ++Kuni;
-        pl.occ = occ;
-        pl.fmt = fmt;
-        pl.warps = W;
-        pl.K = Kshape;
-        pl.Kuniform = Kuni;
-        pl.threads = 32 * W * Kshape;
-        pl.csrBytes = csrBytes;
-        pl.chainBytes = chainBytes;
-        pl.smem = kSmemHeader + csrBytes + static_cast<size_t>(Kshape) * chainBytes;
-        pl.nitems = static_cast<int>(items_for(Kuni));
-        pl.grid = static_cast<int>(std::min<int64_t>(pl.nitems, slots));
-        return RFMF_OK;
-    }
-    return fail(RFMF_ERR_CAPACITY, "no launch plan");
-}
-
-}  // namespace
-
-namespace {
-
-// Per-graph chains per item.  With learned costs c_g (ns per chain-sweep of a
-// CTA slot) for every graph, pick the smallest per-sweep makespan tau such
-// that items of K_g = min(K, floor(tau / c_g)) chains all fit the resident
-// CTA slots; without costs every graph uses the planned K.
-void plan_balanced(rfmf_batch& b) {
-    const size_t G = b.glist.size();
-    bool known = true;
-    for (const rfmf_graph* g : b.glist) known = known && g->costNs > 0.0;
-    if (!known || G < 2) { b.balanced = false; return; }
-    const int64_t slots = static_cast<int64_t>(b.occ) * b.ctx->sms;
-    double lo = 0.0, hi = 0.0;
-    for (const rfmf_graph* g : b.glist) hi = std::max(hi, g->costNs * b.K);
-    auto fits = [&](double tau, std::vector<int>& kg) {
-        int64_t items = 0;
-        for (size_t k = 0; k < G; ++k) {
-            int q = static_cast<int>(std::floor(tau / b.glist[k]->costNs));
-            q = std::max(1, std::min(b.K, q));
-            kg[k] = q;
-            items += (static_cast<int64_t>(b.chainsOf[k].size()) + q - 1) / q;
-        }
-        return items <= slots;
-    };
-    std::vector<int> kg(G, b.K), best(G, b.K);
-    if (!fits(hi, kg)) { b.balanced = false; return; }
-    best = kg;
-    for (int it = 0; it < 60; ++it) {
-        const double mid = 0.5 * (lo + hi);
-        if (fits(mid, kg)) { hi = mid; best = kg; } else { lo = mid; }
-    }
-    b.Kg = best;
-    b.balanced = true;
-}
-
-// Items: graphs in decreasing per-item cost, each graph's chains in groups of
-// its K_g.  Rewrites the host copies; the caller uploads them.
-void build_items(rfmf_batch& b) {
-    const size_t G = b.glist.size();
-    std::vector<int> gorder(G);
-    for (size_t k = 0; k < G; ++k) gorder[k] = static_cast<int>(k);
-    auto itemCost = [&](int k) {
-        const double c = b.glist[k]->costNs > 0.0 ? b.glist[k]->costNs
-                                                    : static_cast<double>(b.glist[k]->n);
-        return c * b.Kg[k];
-    };
-    std::stable_sort(gorder.begin(), gorder.end(), [&](int a, int z) { return itemCost(a) > itemCost(z); });
-    b.items.clear();
-    b.order.clear();
-    for (int gk : gorder) {
-        const auto& cl = b.chainsOf[gk];
-        const size_t K = static_cast<size_t>(b.Kg[gk]);
-        for (size_t s = 0; s < cl.size(); s += K) {
-            DevItem it{};
-            it.graph = gk;
-            it.first = static_cast<int32_t>(b.order.size());
-            it.count = static_cast<int32_t>(std::min(K, cl.size() - s));
-            for (int q = 0; q < it.count; ++q) b.order.push_back(cl[s + q]);
-            b.items.push_back(it);
-        }
-    }
-    b.nitems = static_cast<int>(b.items.size());
-    b.grid = static_cast<int>(std::min<int64_t>(b.nitems, static_cast<int64_t>(b.occ) * b.ctx->sms));
-    b.L.nitems = b.nitems;
-}
-
-// Fold the item timings of completed launches into the graphs' costs.
-int harvest_item_times(rfmf_batch& b) {
-    if (!b.pendingSweeps || b.items.empty()) return RFMF_OK;
-    const uint64_t sweeps = b.pendingSweeps;
-    b.pendingSweeps = 0;
-    std::vector<uint64_t> ns(b.items.size());
-    CU(cudaMemcpy(ns.data(), b.dItemNs.p, ns.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
-    for (size_t i = 0; i < b.items.size(); ++i) {
-        const DevItem& it = b.items[i];
-        if (ns[i] == 0 || it.count <= 0) continue;
-        const double w = static_cast<double>(it.count) * static_cast<double>(sweeps);
-        const double c = static_cast<double>(ns[i]) / w;
-        const rfmf_graph* g = b.glist[it.graph];
-        g->costNs = (g->costNs * g->costWeight + c * w) / (g->costWeight + w);
-        g->costWeight += w;
-    }
-    return RFMF_OK;
-}
-
-}  // namespace
-
-extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph* const* graphs,
-                                 const double* t0s, const uint64_t* solver_seeds,
-                                 const int8_t* initial_spins, int64_t nphases,
-                                 const uint64_t* phases, const uint64_t* iters,
-                                 const rfmf_launch_config* cfg, rfmf_batch** out) {
-    if (!ctx || !out) return fail(RFMF_ERR_INVALID, "ctx/out is NULL");
-    *out = nullptr;
-    if (C <= 0 || C > (int64_t(1) << 30)) return fail(RFMF_ERR_INVALID, "nchains=%lld", (long long)C);
-    if (!graphs || !t0s || !solver_seeds || !initial_spins)
-        return fail(RFMF_ERR_INVALID, "NULL per-chain array");
-    if (nphases < 0 || (nphases > 0 && (!phases || !iters)))
-        return fail(RFMF_ERR_INVALID, "bad phases/iters");
-    rfmf_launch_config dflt{};
-    const rfmf_launch_config& c = cfg ? *cfg : dflt;
-    const int64_t totalAll = rfmf_total_steps(nphases, iters);   // src/host_common.cpp:196-210
-    if (totalAll < 0) return fail(RFMF_ERR_CAPACITY, "iters total more than 10^12 sweeps");
-    uint64_t total = 0, maxP = 0;
-    for (int64_t p = 0; p < nphases; ++p) {
-        if (phases[p] > 0x7FFFFFFFull) return fail(RFMF_ERR_CAPACITY, "phase P too large");
-        if (phases[p]) { total += iters[p]; maxP = std::max<uint64_t>(maxP, phases[p]); }
-    }
-    for (int64_t i = 0; i < C; ++i) {
-        if (!graphs[i] || graphs[i]->ctx != ctx) return fail(RFMF_ERR_INVALID, "graph %lld invalid", (long long)i);
-        if (graphs[i]->n == 0) return fail(RFMF_ERR_INVALID, "chain %lld: graph has no vertices", (long long)i);
-        if (!(t0s[i] > 0.0)) return fail(RFMF_ERR_INVALID, "t0s[%lld] must be > 0", (long long)i);
-    }
-    CU(cudaSetDevice(ctx->device));
-
-    auto b = std::unique_ptr<rfmf_batch>(new (std::nothrow) rfmf_batch());
-    if (!b) return fail(RFMF_ERR_NOMEM, "host allocation failed");
-    b->ctx = ctx;
-    b->C = C;
-    b->total = total;
-
-    // Graph table (distinct graphs in first-use order).
-    std::map<const rfmf_graph*, int> gidx;
-    std::vector<const rfmf_graph*> glist;
-    b->graphOfChain.resize(C);
-    for (int64_t i = 0; i < C; ++i) {
-        auto it = gidx.find(graphs[i]);
-        if (it == gidx.end()) {
-            it = gidx.emplace(graphs[i], static_cast<int>(glist.size())).first;
-            glist.push_back(graphs[i]);
-        }
-        b->graphOfChain[i] = it->second;
-    }
-    int maxN = 0, maxWords = 0;
-    int64_t maxB = 0;
-    for (const rfmf_graph* g : glist) {
-        maxN = std::max<int>(maxN, static_cast<int>(g->n));
-        maxWords = std::max<int>(maxWords, static_cast<int>((g->n + 31) / 32));
-        maxB = std::max(maxB, g->B);
-    }
-
-    // Score path.  The int32 kernel path packs each score with its block
-    // iteration into one int (compact key, see select32), so it needs
-    // (betaMax * B + max|gum| + 1) * 2^kb < 2^31 at every chain's (t0, B, n);
-    // otherwise the launch takes the exact int64 path (the reference's
-    // int64 two-pass route, src/anneal_kernels.cu:348-378).  Either way the
-    // winners are the reference's.
-    if (c.threads_per_chain && c.threads_per_chain != 32 && c.threads_per_chain != 64 &&
-        c.threads_per_chain != 128)
-        return fail(RFMF_ERR_INVALID, "threads_per_chain must be 0, 32, 64 or 128");
-    b->score64 = false;
-    if (c.score_path == 2) b->score64 = true;
-    else {
-        const int T = 32 * choose_warps(maxN, c);
-        for (int64_t i = 0; i < C && !b->score64; ++i)
-            if (!compact_key_safe(static_cast<int64_t>(total), t0s[i], graphs[i]->B,
-                                  key_bits(graphs[i]->n, T)))
-                b->score64 = true;
-        if (b->score64 && c.score_path == 1)
-            return fail(RFMF_ERR_INVALID, "int32 scores would overflow for this (t0, B, sweeps)");
-    }
-
-    // Beta tables over the executed sweeps.
-    BetaTables bt;
-    int rc = build_beta(t0s, C, static_cast<int64_t>(total), bt);
-    if (rc) return rc;
-
-    // Launch plan.
-    b->pmax = static_cast<int>(std::max<uint64_t>(1, std::min<uint64_t>(maxP, static_cast<uint64_t>(maxN))));
-    std::vector<int64_t> perGraph(glist.size(), 0);
-    for (int64_t i = 0; i < C; ++i) ++perGraph[b->graphOfChain[i]];
-    Plan pl{};
-    rc = plan_launch(*b, glist, perGraph, maxN, maxWords, maxB, c, pl);
-    if (rc) return rc;
-    b->dbytes = pl.dbytes;
-    b->fmt = pl.fmt;
-    b->warps = pl.warps;
-    b->K = pl.K;
-    b->threads = pl.threads;
-    b->grid = pl.grid;
-    b->smem = pl.smem;
-
-    std::vector<DevGraph> hg(glist.size());
-    for (size_t k = 0; k < glist.size(); ++k) {
-        const rfmf_graph* g = glist[k];
-        hg[k].offsets = g->offsets.as<uint32_t>();
-        hg[k].edges = g->edges.as<Edge>();
-        hg[k].compact = (pl.fmt == kCsrUnit16) ? g->u16.p : (pl.fmt == kCsrPacked32 ? g->p32.p : nullptr);
-        hg[k].n = static_cast<int32_t>(g->n);
-        hg[k].words = static_cast<int32_t>((g->n + 31) / 32);
-        hg[k].wsum2 = g->wsum2;
-        hg[k].offBytes = g->offBytes;
-        hg[k].entBytes = (pl.fmt == kCsrUnit16) ? g->u16Bytes : (pl.fmt == kCsrPacked32 ? g->p32Bytes : 0);
-    }
-
-    // Work items: each graph's chains in groups of K (or of the per-graph
-    // sizes learned from earlier launches, see rebalance()).
-    b->glist = glist;
-    b->occ = pl.occ;
-    b->chainsOf.assign(glist.size(), {});
-    for (int64_t i = 0; i < C; ++i) b->chainsOf[b->graphOfChain[i]].push_back(static_cast<int32_t>(i));
-    b->Kg.assign(glist.size(), pl.Kuniform);
-    plan_balanced(*b);
-    build_items(*b);
-
-    // Per-chain spin words and initial state.
-    b->chainN.resize(C);
-    b->chainWordOff.resize(C + 1);
-    b->chainWordOff[0] = 0;
-    for (int64_t i = 0; i < C; ++i) {
-        b->chainN[i] = graphs[i]->n;
-        b->chainWordOff[i + 1] = b->chainWordOff[i] + (graphs[i]->n + 31) / 32;
-    }
-    b->words = b->chainWordOff[C];
-    std::vector<uint32_t> bits(static_cast<size_t>(std::max<int64_t>(b->words, 1)), 0u);
-    {
-        size_t sp = 0;
-        for (int64_t i = 0; i < C; ++i) {
-            uint32_t* w = bits.data() + b->chainWordOff[i];
-            for (int64_t v = 0; v < b->chainN[i]; ++v, ++sp)
-                if (initial_spins[sp] >= 0) w[v >> 5] |= 1u << (v & 31);
-        }
-    }
-
-    // Device buffers.
-    if ((rc = b->dGraphs.alloc(hg.size() * sizeof(DevGraph)))) return rc;
-    if ((rc = b->dScheds.alloc(sizeof(DevSchedule)))) return rc;
-    if ((rc = b->dChains.alloc(C * sizeof(DevChain)))) return rc;
-    if ((rc = b->dItems.alloc(C * sizeof(DevItem)))) return rc;
-    if ((rc = b->dItemNs.alloc(C * sizeof(uint64_t)))) return rc;
-    if ((rc = b->dOrder.alloc(C * sizeof(int32_t)))) return rc;
-    if ((rc = b->dPhaseP.alloc(std::max<int64_t>(nphases, 1) * sizeof(uint32_t)))) return rc;
-    if ((rc = b->dPhaseIters.alloc(std::max<int64_t>(nphases, 1) * sizeof(uint64_t)))) return rc;
-    if ((rc = b->dBetaEnd.alloc(bt.end.size() * sizeof(int64_t)))) return rc;
-    if ((rc = b->dBetaVal.alloc(bt.val.size() * sizeof(int32_t)))) return rc;
-    if ((rc = b->dBits.alloc(bits.size() * sizeof(uint32_t)))) return rc;
-    if ((rc = b->dBest.alloc(bits.size() * sizeof(uint32_t)))) return rc;
-    if ((rc = b->dCtl.alloc(4 * sizeof(int32_t)))) return rc;
-
-    std::vector<uint32_t> hp(std::max<int64_t>(nphases, 1), 0);
-    std::vector<uint64_t> hi(std::max<int64_t>(nphases, 1), 0);
-    for (int64_t p = 0; p < nphases; ++p) { hp[p] = static_cast<uint32_t>(phases[p]); hi[p] = iters[p]; }
-    DevSchedule hs{b->dPhaseP.as<uint32_t>(), b->dPhaseIters.as<uint64_t>(),
-                   static_cast<int32_t>(nphases), 0};
-    std::vector<DevChain> hc(C);
-    for (int64_t i = 0; i < C; ++i) {
-        DevChain& d = hc[i];
-        d.graph = static_cast<int32_t>(b->graphOfChain[i]);
-        d.sched = 0;
-        d.solverSeed = solver_seeds[i];
-        d.betaEnd = b->dBetaEnd.as<int64_t>() + bt.chainOff[i];
-        d.betaVal = b->dBetaVal.as<int32_t>() + bt.chainOff[i];
-        d.betaRuns = bt.chainRuns[i];
-        d.spinBits = b->dBits.as<uint32_t>() + b->chainWordOff[i];
-        d.bestBits = b->dBest.as<uint32_t>() + b->chainWordOff[i];
-        d.cur = kUnsetCut;
-        d.best = kUnsetCut;
-        d.sweepsDone = 0;
-        d.sweepsTotal = total;
-        d.improvedSweeps = 0;
-    }
-
-    cudaStream_t st = ctx->stream;
-    CU(cudaMemcpyAsync(b->dGraphs.p, hg.data(), hg.size() * sizeof(DevGraph), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(b->dScheds.p, &hs, sizeof hs, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(b->dChains.p, hc.data(), C * sizeof(DevChain), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(b->dItems.p, b->items.data(), b->items.size() * sizeof(DevItem), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(b->dOrder.p, b->order.data(), C * sizeof(int32_t), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(b->dPhaseP.p, hp.data(), hp.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(b->dPhaseIters.p, hi.data(), hi.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(b->dBetaEnd.p, bt.end.data(), bt.end.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(b->dBetaVal.p, bt.val.data(), bt.val.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(b->dBits.p, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(b->dBest.p, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    CU(cudaMemsetAsync(b->dCtl.p, 0, 4 * sizeof(int32_t), st));
-    CU(cudaStreamSynchronize(st));
-
-    DevLaunch& L = b->L;
-    L.graphs = b->dGraphs.as<DevGraph>();
-    L.scheds = b->dScheds.as<DevSchedule>();
-    L.chains = b->dChains.as<DevChain>();
-    L.items = b->dItems.as<DevItem>();
-    L.order = b->dOrder.as<int32_t>();
-    L.nitems = static_cast<int32_t>(b->items.size());
-    L.itemNs = b->dItemNs.as<uint64_t>();
-    L.ngraphs = static_cast<int32_t>(hg.size());
-    L.nscheds = 1;
-    L.warpsPerChain = pl.warps;
-    L.chainsPerCta = pl.K;
-    L.maxN = maxN;
-    L.maxWords = maxWords;
-    L.pmax = b->pmax;
-    L.csrBytes = pl.csrBytes;
-    L.chainBytes = pl.chainBytes;
-    L.queue = b->dCtl.as<int32_t>();
-    L.error = b->dCtl.as<int32_t>() + 1;
-    L.errorItem = b->dCtl.as<int32_t>() + 2;
-    L.window = 0;
-    std::memcpy(L.lut, ctx->lut, sizeof L.lut);
-    *out = b.release();
-    return RFMF_OK;
-}
-
-namespace {
-int enqueue_run(rfmf_batch* b, uint64_t sweeps, bool capturing = false) {
-    if (!capturing && !b->balanced) {
-        plan_balanced(*b);
-        if (b->balanced) {
-            build_items(*b);
-            // Stream-ordered after any launch still reading the old items.
-            CU(cudaMemcpyAsync(b->dItems.p, b->items.data(), b->items.size() * sizeof(DevItem),
-                               cudaMemcpyHostToDevice, b->ctx->stream));
-            CU(cudaMemcpyAsync(b->dOrder.p, b->order.data(), b->order.size() * sizeof(int32_t),
-                               cudaMemcpyHostToDevice, b->ctx->stream));
-            CU(cudaMemsetAsync(b->dItemNs.p, 0, b->items.size() * sizeof(uint64_t), b->ctx->stream));
-        }
-    }
-    DevLaunch L = b->L;
-    L.window = sweeps;
-    if (!capturing) {
-        const uint64_t adv = std::min<uint64_t>(sweeps, b->total - std::min(b->total, b->hostDone));
-        b->hostDone += adv;
-        b->pendingSweeps = adv;
-    }
-    CU(cudaMemsetAsync(L.queue, 0, sizeof(int32_t), b->ctx->stream));
-    CU(launch_anneal(L, b->dbytes, b->fmt, b->score64, b->grid, b->threads, b->smem,
-                     b->ctx->stream));
-    return RFMF_OK;
-}
-}  // namespace
-extern "C" int rfmf_batch_run(rfmf_batch* b, uint64_t sweeps) {
-    if (!b) return fail(RFMF_ERR_INVALID, "batch is NULL");
-    CU(cudaSetDevice(b->ctx->device));
-    return enqueue_run(b, sweeps);
-}
-
-extern "C" int rfmf_batch_run_graph(rfmf_batch* b, uint64_t sweeps, int launches, int replays) {
-    if (!b || launches <= 0 || replays < 0) return fail(RFMF_ERR_INVALID, "bad arguments");
-    CU(cudaSetDevice(b->ctx->device));
-    if (!b->graphExec || b->graphSweeps != sweeps || b->graphLaunches != launches) {
-        if (b->graphExec) { cudaGraphExecDestroy(b->graphExec); b->graphExec = nullptr; }
-        cudaGraph_t graph = nullptr;
-        CU(cudaStreamBeginCapture(b->ctx->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = RFMF_OK;
-        for (int i = 0; i < launches && rc == RFMF_OK; ++i) rc = enqueue_run(b, sweeps, true);
-        const cudaError_t ec = cudaStreamEndCapture(b->ctx->stream, &graph);
-        if (rc != RFMF_OK) { if (graph) cudaGraphDestroy(graph); return rc; }
-        if (ec != cudaSuccess) return fail(RFMF_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ec));
-        const cudaError_t ei = cudaGraphInstantiate(&b->graphExec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (ei != cudaSuccess) { b->graphExec = nullptr; return fail(RFMF_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(ei)); }
-        b->graphSweeps = sweeps;
-        b->graphLaunches = launches;
-    }
-    for (int r = 0; r < replays; ++r) {
-        CU(cudaGraphLaunch(b->graphExec, b->ctx->stream));
-        for (int i = 0; i < launches; ++i)
-            b->hostDone += std::min<uint64_t>(sweeps, b->total - std::min(b->total, b->hostDone));
-    }
-    b->pendingSweeps = 0;   // item times of replayed launches are not harvested
-    return RFMF_OK;
-}
-
-extern "C" int rfmf_batch_run_timed(rfmf_batch* b, uint64_t sweeps, float* ms) {
-    if (!b || !ms) return fail(RFMF_ERR_INVALID, "batch/ms is NULL");
-    CU(cudaSetDevice(b->ctx->device));
-    cudaEvent_t e0, e1;
-    CU(cudaEventCreate(&e0));
-    CU(cudaEventCreate(&e1));
-    int rc = RFMF_OK;
-    if (cudaEventRecord(e0, b->ctx->stream) != cudaSuccess) rc = fail(RFMF_ERR_CUDA, "event record failed");
-    if (!rc) rc = enqueue_run(b, sweeps);
-    if (!rc && cudaEventRecord(e1, b->ctx->stream) != cudaSuccess) rc = fail(RFMF_ERR_CUDA, "event record failed");
-    if (!rc) rc = rfmf_batch_synchronize(b);
-    if (!rc && cudaEventElapsedTime(ms, e0, e1) != cudaSuccess) rc = fail(RFMF_ERR_CUDA, "event elapsed failed");
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    return rc;
-}
-
-extern "C" int rfmf_batch_stats(rfmf_batch* b, uint64_t* improved_sweeps) {
-    if (!b || !improved_sweeps) return fail(RFMF_ERR_INVALID, "batch/out is NULL");
-    CU(cudaSetDevice(b->ctx->device));
-    CU(cudaStreamSynchronize(b->ctx->stream));
-    std::vector<DevChain> hc(b->C);
-    CU(cudaMemcpy(hc.data(), b->dChains.p, b->C * sizeof(DevChain), cudaMemcpyDeviceToHost));
-    for (int64_t i = 0; i < b->C; ++i) improved_sweeps[i] = hc[i].improvedSweeps;
-    return RFMF_OK;
-}
-
-extern "C" int rfmf_batch_synchronize(rfmf_batch* b) {
-    if (!b) return fail(RFMF_ERR_INVALID, "batch is NULL");
-    CU(cudaSetDevice(b->ctx->device));
-    CU(cudaStreamSynchronize(b->ctx->stream));
-    if (int rc = harvest_item_times(*b)) return rc;
-    int32_t ctl[4];
-    CU(cudaMemcpy(ctl, b->dCtl.p, sizeof ctl, cudaMemcpyDeviceToHost));
-    if (ctl[1] != kDevOk) {
-        static const char* names[] = {"ok", "carried cut value disagrees with the spins",
-                                      "beta table shorter than the window", "bad work item"};
-        const int code = ctl[1];
-        return fail(RFMF_ERR_DEVICE, "device error %d (%s) on chain %d", code,
-                    (code >= 0 && code < 4) ? names[code] : "?", ctl[2]);
-    }
-    return RFMF_OK;
-}
-
-extern "C" int rfmf_batch_read(rfmf_batch* b, int8_t* end_spins, int8_t* best_spins,
-                               int64_t* cur_vals, int64_t* best_vals, uint64_t* sweeps_done) {
-    if (!b) return fail(RFMF_ERR_INVALID, "batch is NULL");
-    int rc = rfmf_batch_synchronize(b);
-    if (rc) return rc;
-    std::vector<DevChain> hc(b->C);
-    CU(cudaMemcpy(hc.data(), b->dChains.p, b->C * sizeof(DevChain), cudaMemcpyDeviceToHost));
-    auto unpack = [&](const DevBuf& src, int8_t* dst) -> int {
-        std::vector<uint32_t> w(static_cast<size_t>(std::max<int64_t>(b->words, 1)));
-        CU(cudaMemcpy(w.data(), src.p, w.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-        size_t sp = 0;
-        for (int64_t i = 0; i < b->C; ++i) {
-            const uint32_t* cw = w.data() + b->chainWordOff[i];
-            for (int64_t v = 0; v < b->chainN[i]; ++v, ++sp)
-                dst[sp] = ((cw[v >> 5] >> (v & 31)) & 1u) ? 1 : -1;
-        }
-        return RFMF_OK;
-    };
-    if (end_spins && (rc = unpack(b->dBits, end_spins))) return rc;
-    if (best_spins && (rc = unpack(b->dBest, best_spins))) return rc;
-    for (int64_t i = 0; i < b->C; ++i) {
-        if (cur_vals) cur_vals[i] = hc[i].cur;
-        if (best_vals) best_vals[i] = hc[i].best;
-        if (sweeps_done) sweeps_done[i] = hc[i].sweepsDone;
-    }
-    return RFMF_OK;
-}
-
-extern "C" int rfmf_batch_cuts(rfmf_batch* b, int which, int64_t* out_cuts) {
-    if (!b || !out_cuts || (which != 0 && which != 1)) return fail(RFMF_ERR_INVALID, "bad arguments");
-    if (int rc = rfmf_batch_synchronize(b)) return rc;
-    DevBuf d;
-    if (int rc = d.alloc(b->C * sizeof(int64_t))) return rc;
-    CU(launch_chain_cuts(b->L.chains, b->L.graphs, static_cast<int>(b->C), which, d.as<int64_t>(),
-                         b->ctx->stream));
-    CU(cudaMemcpyAsync(out_cuts, d.p, b->C * sizeof(int64_t), cudaMemcpyDeviceToHost, b->ctx->stream));
-    CU(cudaStreamSynchronize(b->ctx->stream));
-    return RFMF_OK;
-}
-
-extern "C" int rfmf_batch_partitions(rfmf_batch* b, int which, char* out, int64_t stride) {
-    if (!b || !out || (which != 0 && which != 1)) return fail(RFMF_ERR_INVALID, "bad arguments");
-    int64_t maxN = 0;
-    for (int64_t n : b->chainN) maxN = std::max(maxN, n);
-    if (stride < maxN) return fail(RFMF_ERR_INVALID, "stride %lld < largest n %lld", (long long)stride, (long long)maxN);
-    if (int rc = rfmf_batch_synchronize(b)) return rc;
-    // chunks of chains bounded to ~256 MB of device staging
-    const int64_t per = std::max<int64_t>(1, std::min<int64_t>(b->C, (int64_t(256) << 20) / std::max<int64_t>(stride, 1)));
-    DevBuf d;
-    if (int rc = d.alloc(static_cast<size_t>(per * stride))) return rc;
-    for (int64_t c0 = 0; c0 < b->C; c0 += per) {
-        const int64_t cnt = std::min(per, b->C - c0);
-        CU(cudaMemsetAsync(d.p, 0, static_cast<size_t>(cnt * stride), b->ctx->stream));
-        CU(launch_chain_partitions(b->L.chains, b->L.graphs, static_cast<int>(c0), static_cast<int>(cnt),
-                                   static_cast<int>(maxN), which, d.as<char>(), stride, b->ctx->stream));
-        CU(cudaMemcpyAsync(out + c0 * stride, d.p, static_cast<size_t>(cnt * stride), cudaMemcpyDeviceToHost,
-                           b->ctx->stream));
-        CU(cudaStreamSynchronize(b->ctx->stream));
-    }
-    return RFMF_OK;
-}
-
-extern "C" int rfmf_batch_info(const rfmf_batch* b, rfmf_batch_plan* out) {
-    if (!b || !out) return fail(RFMF_ERR_INVALID, "batch/out is NULL");
-    out->nchains = b->C;
-    out->total_sweeps = b->total;
-    out->threads_per_chain = 32 * b->warps;
-    out->chains_per_cta = b->K;
-    out->grid = b->grid;
-    out->items = b->nitems;
-    out->score64 = b->score64 ? 1 : 0;
-    out->csr_format = b->fmt + 1;
-    out->gain_width = b->dbytes;
-    out->smem_bytes = static_cast<int>(b->smem);
-    out->balanced = b->balanced ? 1 : 0;
-    return RFMF_OK;
-}
-
-extern "C" int rfmf_batch_destroy(rfmf_batch* b) {
-    if (!b) return RFMF_OK;
-    cudaSetDevice(b->ctx->device);
-    delete b;
-    return RFMF_OK;
-}
-
-// ---------------------------------------------------------------- anneal
-extern "C" int rfmf_anneal(rfmf_context* ctx, const rfmf_graph* g, int64_t max_weighted_deg,
-                           int64_t C, const int8_t* initial_spins, const double* t0s,
-                           int64_t nphases, const uint64_t* phases, const uint64_t* iters,
-                           const uint64_t* solver_seeds, const rfmf_launch_config* cfg,
-                           int8_t* end_spins, int8_t* best_spins, float* kernel_ms,
-                           int64_t* kernel_best_vals, int64_t* kernel_final_vals) {
-    if (!ctx || !g) return fail(RFMF_ERR_INVALID, "ctx/graph is NULL");
-    if (C <= 0 || !initial_spins || !t0s || !solver_seeds)
-        return fail(RFMF_ERR_INVALID, "annealGpu needs C > 0 and per-chain arrays");
-    (void)max_weighted_deg;   // the graph carries B; accepted for signature parity
-    const int64_t n = g->n;
-    if (kernel_ms) *kernel_ms = 0.0f;
-    if (n == 0 || nphases == 0) {
-        // src/anneal_kernels.cu:856-868: inputs returned, cutValueCsr values.
-        std::vector<uint32_t> off(n + 1, 0);
-        for (int64_t c = 0; c < C; ++c) {
-            if (end_spins) std::memcpy(end_spins + c * n, initial_spins + c * n, n);
-            if (best_spins) std::memcpy(best_spins + c * n, initial_spins + c * n, n);
-            if (kernel_best_vals) kernel_best_vals[c] = 0;
-            if (kernel_final_vals) kernel_final_vals[c] = 0;
-        }
-        if (n > 0) {
-            // Cut values need the host CSR, which the device graph no longer
-            // has; recompute from the device copy.
-            std::vector<uint32_t> ho(n + 1);
-            std::vector<Edge> he(g->m * 2);
-            CU(cudaMemcpy(ho.data(), g->offsets.p, (n + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-            if (!he.empty()) CU(cudaMemcpy(he.data(), g->edges.p, he.size() * sizeof(Edge), cudaMemcpyDeviceToHost));
-            for (int64_t c = 0; c < C; ++c) {
-                int64_t v = 0;
-                const int8_t* s = initial_spins + c * n;
-                for (int64_t x = 0; x < n; ++x)
-                    for (uint32_t i = ho[x]; i < ho[x + 1]; ++i)
-                        if (he[i].col > x && s[x] != s[he[i].col]) v += he[i].w;
-                if (kernel_best_vals) kernel_best_vals[c] = v;
-                if (kernel_final_vals) kernel_final_vals[c] = v;
-            }
-        }
-        return RFMF_OK;
-    }
-    std::vector<const rfmf_graph*> gs(C, g);
-    rfmf_batch* b = nullptr;
-    int rc = rfmf_batch_create(ctx, C, gs.data(), t0s, solver_seeds, initial_spins, nphases,
-                               phases, iters, cfg, &b);
-    if (rc) return rc;
-    std::unique_ptr<rfmf_batch, int (*)(rfmf_batch*)> guard(b, rfmf_batch_destroy);
-    cudaEvent_t e0, e1;
-    CU(cudaEventCreate(&e0));
-    CU(cudaEventCreate(&e1));
-    CU(cudaEventRecord(e0, ctx->stream));
-    rc = enqueue_run(b, b->total);
-    if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
-    CU(cudaEventRecord(e1, ctx->stream));
-    rc = rfmf_batch_synchronize(b);
-    float ms = 0.0f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (rc) return rc;
-    if (kernel_ms) *kernel_ms = ms;
-    return rfmf_batch_read(b, end_spins, best_spins, kernel_final_vals, kernel_best_vals, nullptr);
-}
 

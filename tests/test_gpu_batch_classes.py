@@ -1,0 +1,66 @@
+"""Batches whose graphs fall into several launch classes (gain width, CSR
+format, warps per chain, score path): each class runs as its own
+persistent launch on its own stream, and every chain must still equal a
+standalone anneal of its graph bit for bit -- also when the windows are
+replayed from a captured CUDA graph."""
+import numpy as np
+import pytest
+
+from conftest import chains_for
+
+pytestmark = pytest.mark.gpu
+
+
+def _graphs(rfmf):
+    heavy = rfmf.erdos_renyi(260, 0.05, signed=True, seed=6)
+    heavy.weight = heavy.weight * 9          # B > 127: int32 gains
+    return [
+        rfmf.erdos_renyi(300, 0.04, signed=True, seed=1),     # small, unit16
+        rfmf.torus(60, 150, signed=True, seed=2),             # n = 9000: W = 2
+        rfmf.planar_like(1500, seed=3),                       # +1 weights
+        heavy,
+    ]
+
+
+def _run(rfmf, ctx, graphs, t0_of, phases, iters, use_graph):
+    dgs = [rfmf.DeviceGraph(ctx, g) for g in graphs]
+    per = []
+    gl, ini, sol, t0 = [], [], [], []
+    for k, g in enumerate(graphs):
+        seeds = list(range(1000 * k, 1000 * k + 12))
+        init, solver = chains_for(g, seeds)
+        ts = [t0_of(k, i) for i in range(12)]
+        per.append((init, solver, ts))
+        gl += [dgs[k]] * 12
+        ini += list(init)
+        sol += solver
+        t0 += ts
+    b = rfmf.Batch(ctx, gl, t0, sol, ini, phases, iters)
+    info = b.info()
+    total = sum(i for p, i in zip(phases, iters) if p)
+    if use_graph:
+        b.run_graph(total // 4, launches=2, replays=2)
+    else:
+        b.run(total // 3)
+        b.run(total)
+    r = b.read()
+    b.close()
+    return dgs, per, info, r
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_multi_class_batch_matches_standalone(rfmf, ctx, use_graph):
+    graphs = _graphs(rfmf)
+    phases, iters = [64, 8, 1], [200, 200, 200]
+    # graph 0 chains 0-3 at a tiny t0 force the int64 score path for graph 0
+    t0_of = lambda k, i: 0.004 if (k == 0 and i < 4) else 50.0 + 10 * i
+    dgs, per, info, r = _run(rfmf, ctx, graphs, t0_of, phases, iters, use_graph)
+    assert info["launch_classes"] >= 3, info
+    for k, g in enumerate(graphs):
+        init, solver, ts = per[k]
+        ref = rfmf.anneal_gpu(ctx, dgs[k], g.max_weighted_degree(), init, ts, phases, iters, solver)
+        sl = slice(12 * k, 12 * k + 12)
+        assert np.array_equal(np.stack(r["best_spins"][sl]), ref.best_spins), k
+        assert np.array_equal(np.stack(r["end_spins"][sl]), ref.end_spins), k
+        assert np.array_equal(r["best_vals"][sl], ref.best_vals), k
+        assert np.array_equal(r["cur_vals"][sl], ref.final_vals), k
