@@ -207,6 +207,32 @@ def cpu_rate(graphs, steps, warmup, target_s, rank_seed_base=0):
     return cs / el, cores, sample, el
 
 
+def cpu_config1(target_s):
+    """The plain-method small case on the CPU restatement: ER n = 800, p = 0.06,
+    +1 weights, 32 chains (raw seeds 0..31, t0 ladder), the default schedule
+    compressed to a bounded sweep count, one chain per core."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as ora
+    import rfmf_gb300 as R
+    ora.lib()
+    cores = ora.default_threads()
+    g = R.erdos_renyi(800, 0.06, seed=0, name="er800_p0.06")
+    seeds = list(range(32))
+    init = np.stack([R.initial_spins(x, g.n) for x in seeds])
+    t0s = [LADDER[i % 8] for i in range(32)]
+    sol = [R.solver_seed(x) for x in seeds]
+    t = time.perf_counter()
+    ora.anneal(g, init[:cores], t0s[:cores], sol[:cores], PHASES, [64] * 8, nthreads=cores)
+    per = (time.perf_counter() - t) / (512 * max(1, min(cores, 32) // cores))
+    sweeps = max(800, int(target_s / max(per, 1e-7) * cores / 32 / 8) * 8)
+    t = time.perf_counter()
+    ora.anneal(g, init, t0s, sol, PHASES, [sweeps // 8] * 8, nthreads=cores)
+    el = time.perf_counter() - t
+    return {"value": 32 * sweeps / el, "unit": "chain-steps/s", "cores": cores, "kind": "port",
+            "sample": f"ER n=800 p=0.06 +1, 32 chains x {sweeps} sweeps (phases 128..1), "
+                      f"{el:.1f} s"}
+
+
 # --------------------------------------------------------------- GPU arm
 def gpu_arm(args, rank, world):
     import torch
@@ -702,6 +728,7 @@ def main():
         rate, cores, sample, _ = cpu_rate(workload_graphs(), 1, 0, args.cpu_seconds)
         res["cpu_baseline"] = {"value": rate, "unit": "chain-steps/s", "cores": cores,
                                "kind": "port", "sample": sample}
+        res["cpu_config1"] = cpu_config1(min(6.0, args.cpu_seconds))
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

@@ -11,7 +11,11 @@ cut values and the sha256 of both partition strings ("0"/"1" per vertex, the
 log's format) are compared with the committed values and the outcome is
 merged into tests/golden/committed_log_pin.json under "gpu_entries".
 
-Usage: pin_committed_logs_gpu.py SPEC.json GSET_DIR [--window N]
+With --device-ingest the graphs are read by the native parser
+(rfmf_gset_parse) and their CSR is built on the GPU (rfmf_graph_from_edges)
+instead of by the Python reader, so the rerun also covers the ingest path.
+
+Usage: pin_committed_logs_gpu.py SPEC.json GSET_DIR [--window N] [--device-ingest]
 """
 import argparse
 import hashlib
@@ -40,6 +44,7 @@ def main():
     ap.add_argument("spec")
     ap.add_argument("gset_dir")
     ap.add_argument("--window", type=int, default=5_000_000)
+    ap.add_argument("--device-ingest", action="store_true")
     a = ap.parse_args()
 
     import rfmf_gb300 as R
@@ -52,11 +57,22 @@ def main():
 
     ctx = R.Context(0)
     graphs, dgs = {}, {}
+    class Shape:   # n of a device-built graph (the host never holds its CSR)
+        def __init__(self, n):
+            self.n = n
+
     for c in spec:
         if c["graph"] not in graphs:
-            g = R.read_gset(pathlib.Path(a.gset_dir) / c["graph"], name=c["graph"])
-            graphs[c["graph"]] = g
-            dgs[c["graph"]] = R.DeviceGraph(ctx, g)
+            path = pathlib.Path(a.gset_dir) / c["graph"]
+            if a.device_ingest:
+                d = R.parse_gset(path)
+                dg = R.DeviceGraph.from_edges(ctx, d["u"], d["v"], d["w"])
+                graphs[c["graph"]] = Shape(dg.n)
+                dgs[c["graph"]] = dg
+            else:
+                g = R.read_gset(path, name=c["graph"])
+                graphs[c["graph"]] = g
+                dgs[c["graph"]] = R.DeviceGraph(ctx, g)
     init = [R.initial_spins(c["seed"], graphs[c["graph"]].n) for c in spec]
     b = R.Batch(ctx, [dgs[c["graph"]] for c in spec], [c["t0"] for c in spec],
                 [R.solver_seed(c["seed"]) for c in spec], init, phases, iters)
@@ -92,7 +108,9 @@ def main():
     import torch
     record["gpu_run"] = dict(device=torch.cuda.get_device_name(0), sm_count=ctx.info()["sm_count"],
                              chains=len(entries), sweeps_per_chain=total,
-                             seconds=round(el, 1), window=a.window)
+                             seconds=round(el, 1), window=a.window,
+                             ingest="native parser + CSR built on the GPU" if a.device_ingest
+                             else "Python reader + host CSR")
     OUT.write_text(json.dumps(record, indent=1) + "\n")
     return 0 if nmatch == len(entries) else 1
 

@@ -92,6 +92,20 @@ def test_er800_config1_shape(rfmf, ctx, oracle):
     assert_same(res, o, "er800")
 
 
+def test_large_sparse_config3_shapes(rfmf, ctx, oracle):
+    """The large sparse shapes: 100x200 torus (n = 20000, +-1; its CSR does not
+    fit shared memory beside a chain, so it walks HBM with four warps per
+    chain), a random tree n = 10000 (+1) and ER n = 5000 mean degree 5 (+-1),
+    all phases of the default schedule, against the oracle."""
+    graphs = [rfmf.torus(100, 200, signed=True, seed=0),
+              rfmf.random_tree(10000, seed=0),
+              rfmf.erdos_renyi_sparse(5000, 5, signed=True, seed=0)]
+    for g in graphs:
+        res, o = run_pair(rfmf, ctx, oracle, g, [3, 4], [35.0, 400.0],
+                          [128, 64, 32, 16, 8, 4, 2, 1], [12] * 8)
+        assert_same(res, o, g.name)
+
+
 def test_int64_score_path(rfmf, ctx, oracle):
     """t0 = 0.01 fails the int32 gate (tests/test_chain_isolation.sh:129-131):
     the whole launch takes the int64 score path."""
