@@ -340,7 +340,11 @@ def gpu_arm(args, rank, world):
         for e in tt:
             e["plain_seconds_est"] = e["sweeps"] * len(graphs) * args.chains / plain["value"]
     batched = None if args.no_batched else batched_arm(args, ctx)
-    serving = None if args.no_serving else serving_arm(args, ctx)
+    serving = None
+    if not args.no_serving:
+        rates = [float(x) for x in str(args.serve_rate).split(",") if x]
+        runs = [serving_arm(args, ctx, r) for r in rates]
+        serving = runs[0] if len(runs) == 1 else runs
 
     peaks = measured_peaks()
     sm_count = ctx.info()["sm_count"]
@@ -564,7 +568,7 @@ def serving_graphs():
     return out
 
 
-def serving_arm(args, ctx):
+def serving_arm(args, ctx, rate):
     """Continuous batching through the request server: Poisson arrivals at
     `rate` req/s for `seconds`; each request draws a graph from the
     large-sparse families (torus, tree, ER d=5; n 5000-20000), 16-256 chains
@@ -576,7 +580,7 @@ def serving_arm(args, ctx):
     graphs = serving_graphs()
     dgs = [R.DeviceGraph(ctx, g) for g in graphs]
     rng = np.random.default_rng(17)
-    rate, seconds = args.serve_rate, args.serve_seconds
+    seconds = args.serve_seconds
     arrivals = []
     t = 0.0
     while True:
@@ -687,7 +691,7 @@ def main():
     ap.add_argument("--batched-graphs", type=int, default=512)
     ap.add_argument("--batched-sweeps", type=int, default=2000)
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--serve-rate", type=float, default=2.0)
+    ap.add_argument("--serve-rate", default="2", help="req/s; a comma list sweeps several rates")
     ap.add_argument("--serve-seconds", type=float, default=20.0)
     ap.add_argument("--serve-sweeps", type=int, default=100_000)
     ap.add_argument("--serve-window", type=int, default=4096)

@@ -306,7 +306,7 @@ int enqueue_run(rfmf_batch* b, uint64_t sweeps, bool capturing = false) {
 
 }  // namespace
 
-extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph* const* graphs,
+static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph* const* graphs,
                                  const double* t0s, const uint64_t* solver_seeds,
                                  const int8_t* initial_spins, int64_t nphases,
                                  const uint64_t* phases, const uint64_t* iters,
@@ -390,10 +390,19 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
         const uint32_t chainB = chain_layout(static_cast<int>(g->n), static_cast<int>((g->n + 31) / 32), pmaxG, W,
                                              dbytes).total;
         int fmt = kCsrGlobal;
+        // A shared-memory CSR pays only while it leaves room for the chains a
+        // CTA should hold: about 8 warps, fewer when the graph has fewer
+        // chains or the batch fewer than that per SM.  Otherwise its rows are
+        // walked in HBM (L2-resident) and the CTA holds more chains.
+        const int64_t perSm = (b->C + ctx->sms - 1) / std::max(ctx->sms, 1);
+        const int64_t kWant = std::max<int64_t>(
+            1, std::min<int64_t>({static_cast<int64_t>(chainsOfGraph[gi].size()),
+                                  static_cast<int64_t>(std::max(1, 8 / W)), perSm}));
         auto fits = [&](int f) {
             cudaFuncAttributes fa{};
             const int64_t dynMax = dyn_smem_max(ctx, kernel_ptr(dbytes, f, s64), fa);
-            return dynMax > 0 && static_cast<int64_t>(kSmemHeader) + csr_bytes(g, f) + chainB <= dynMax;
+            return dynMax > 0 &&
+                   static_cast<int64_t>(kSmemHeader) + csr_bytes(g, f) + kWant * chainB <= dynMax;
         };
         if (c.csr_format == 1) {
             if (!g->unit16) return fail(RFMF_ERR_INVALID, "unit16 CSR needs |w| == 1 and n <= 32768");
@@ -551,13 +560,13 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
     return RFMF_OK;
 }
 
-extern "C" int rfmf_batch_run(rfmf_batch* b, uint64_t sweeps) {
+static int rfmf_batch_run_impl(rfmf_batch* b, uint64_t sweeps) {
     if (!b) return fail(RFMF_ERR_INVALID, "batch is NULL");
     CU(cudaSetDevice(b->ctx->device));
     return enqueue_run(b, sweeps);
 }
 
-extern "C" int rfmf_batch_run_graph(rfmf_batch* b, uint64_t sweeps, int launches, int replays) {
+static int rfmf_batch_run_graph_impl(rfmf_batch* b, uint64_t sweeps, int launches, int replays) {
     if (!b || launches <= 0 || replays < 0) return fail(RFMF_ERR_INVALID, "bad arguments");
     CU(cudaSetDevice(b->ctx->device));
     if (!b->graphExec || b->graphSweeps != sweeps || b->graphLaunches != launches) {
@@ -584,7 +593,7 @@ extern "C" int rfmf_batch_run_graph(rfmf_batch* b, uint64_t sweeps, int launches
     return RFMF_OK;
 }
 
-extern "C" int rfmf_batch_run_timed(rfmf_batch* b, uint64_t sweeps, float* ms) {
+static int rfmf_batch_run_timed_impl(rfmf_batch* b, uint64_t sweeps, float* ms) {
     if (!b || !ms) return fail(RFMF_ERR_INVALID, "batch/ms is NULL");
     CU(cudaSetDevice(b->ctx->device));
     cudaEvent_t e0, e1;
@@ -601,7 +610,7 @@ extern "C" int rfmf_batch_run_timed(rfmf_batch* b, uint64_t sweeps, float* ms) {
     return rc;
 }
 
-extern "C" int rfmf_batch_stats(rfmf_batch* b, uint64_t* improved_sweeps) {
+static int rfmf_batch_stats_impl(rfmf_batch* b, uint64_t* improved_sweeps) {
     if (!b || !improved_sweeps) return fail(RFMF_ERR_INVALID, "batch/out is NULL");
     CU(cudaSetDevice(b->ctx->device));
     CU(cudaStreamSynchronize(b->ctx->stream));
@@ -611,7 +620,7 @@ extern "C" int rfmf_batch_stats(rfmf_batch* b, uint64_t* improved_sweeps) {
     return RFMF_OK;
 }
 
-extern "C" int rfmf_batch_synchronize(rfmf_batch* b) {
+static int rfmf_batch_synchronize_impl(rfmf_batch* b) {
     if (!b) return fail(RFMF_ERR_INVALID, "batch is NULL");
     CU(cudaSetDevice(b->ctx->device));
     CU(cudaStreamSynchronize(b->ctx->stream));
@@ -631,7 +640,7 @@ extern "C" int rfmf_batch_synchronize(rfmf_batch* b) {
     return RFMF_OK;
 }
 
-extern "C" int rfmf_batch_read(rfmf_batch* b, int8_t* end_spins, int8_t* best_spins,
+static int rfmf_batch_read_impl(rfmf_batch* b, int8_t* end_spins, int8_t* best_spins,
                                int64_t* cur_vals, int64_t* best_vals, uint64_t* sweeps_done) {
     if (!b) return fail(RFMF_ERR_INVALID, "batch is NULL");
     int rc = rfmf_batch_synchronize(b);
@@ -659,7 +668,7 @@ extern "C" int rfmf_batch_read(rfmf_batch* b, int8_t* end_spins, int8_t* best_sp
     return RFMF_OK;
 }
 
-extern "C" int rfmf_batch_cuts(rfmf_batch* b, int which, int64_t* out_cuts) {
+static int rfmf_batch_cuts_impl(rfmf_batch* b, int which, int64_t* out_cuts) {
     if (!b || !out_cuts || (which != 0 && which != 1)) return fail(RFMF_ERR_INVALID, "bad arguments");
     if (int rc = rfmf_batch_synchronize(b)) return rc;
     DevBuf d;
@@ -671,7 +680,7 @@ extern "C" int rfmf_batch_cuts(rfmf_batch* b, int which, int64_t* out_cuts) {
     return RFMF_OK;
 }
 
-extern "C" int rfmf_batch_partitions(rfmf_batch* b, int which, char* out, int64_t stride) {
+static int rfmf_batch_partitions_impl(rfmf_batch* b, int which, char* out, int64_t stride) {
     if (!b || !out || (which != 0 && which != 1)) return fail(RFMF_ERR_INVALID, "bad arguments");
     int64_t maxN = 0;
     for (int64_t n : b->chainN) maxN = std::max(maxN, n);
@@ -731,7 +740,7 @@ extern "C" int rfmf_batch_destroy(rfmf_batch* b) {
 }
 
 // ---------------------------------------------------------------- anneal
-extern "C" int rfmf_anneal(rfmf_context* ctx, const rfmf_graph* g, int64_t max_weighted_deg,
+static int rfmf_anneal_impl(rfmf_context* ctx, const rfmf_graph* g, int64_t max_weighted_deg,
                            int64_t C, const int8_t* initial_spins, const double* t0s,
                            int64_t nphases, const uint64_t* phases, const uint64_t* iters,
                            const uint64_t* solver_seeds, const rfmf_launch_config* cfg,
@@ -790,4 +799,115 @@ extern "C" int rfmf_anneal(rfmf_context* ctx, const rfmf_graph* g, int64_t max_w
     if (rc) return rc;
     if (kernel_ms) *kernel_ms = ms;
     return rfmf_batch_read(b, end_spins, best_spins, kernel_final_vals, kernel_best_vals, nullptr);
+}
+
+// C ABI entry points: no C++ exception crosses the boundary.
+extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph* const* graphs,
+                                 const double* t0s, const uint64_t* solver_seeds,
+                                 const int8_t* initial_spins, int64_t nphases,
+                                 const uint64_t* phases, const uint64_t* iters,
+                                 const rfmf_launch_config* cfg, rfmf_batch** out) {
+    try {
+        return rfmf_batch_create_impl(ctx, C, graphs, t0s, solver_seeds, initial_spins, nphases, phases, iters, cfg, out);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_batch_create");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_batch_create");
+    }
+}
+
+extern "C" int rfmf_batch_read(rfmf_batch* b, int8_t* end_spins, int8_t* best_spins,
+                               int64_t* cur_vals, int64_t* best_vals, uint64_t* sweeps_done) {
+    try {
+        return rfmf_batch_read_impl(b, end_spins, best_spins, cur_vals, best_vals, sweeps_done);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_batch_read");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_batch_read");
+    }
+}
+
+extern "C" int rfmf_batch_run(rfmf_batch* b, uint64_t sweeps) {
+    try {
+        return rfmf_batch_run_impl(b, sweeps);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_batch_run");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_batch_run");
+    }
+}
+
+extern "C" int rfmf_batch_run_graph(rfmf_batch* b, uint64_t sweeps, int launches, int replays) {
+    try {
+        return rfmf_batch_run_graph_impl(b, sweeps, launches, replays);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_batch_run_graph");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_batch_run_graph");
+    }
+}
+
+extern "C" int rfmf_batch_run_timed(rfmf_batch* b, uint64_t sweeps, float* ms) {
+    try {
+        return rfmf_batch_run_timed_impl(b, sweeps, ms);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_batch_run_timed");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_batch_run_timed");
+    }
+}
+
+extern "C" int rfmf_batch_stats(rfmf_batch* b, uint64_t* improved_sweeps) {
+    try {
+        return rfmf_batch_stats_impl(b, improved_sweeps);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_batch_stats");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_batch_stats");
+    }
+}
+
+extern "C" int rfmf_batch_synchronize(rfmf_batch* b) {
+    try {
+        return rfmf_batch_synchronize_impl(b);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_batch_synchronize");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_batch_synchronize");
+    }
+}
+
+extern "C" int rfmf_batch_cuts(rfmf_batch* b, int which, int64_t* out_cuts) {
+    try {
+        return rfmf_batch_cuts_impl(b, which, out_cuts);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_batch_cuts");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_batch_cuts");
+    }
+}
+
+extern "C" int rfmf_batch_partitions(rfmf_batch* b, int which, char* out, int64_t stride) {
+    try {
+        return rfmf_batch_partitions_impl(b, which, out, stride);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_batch_partitions");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_batch_partitions");
+    }
+}
+
+extern "C" int rfmf_anneal(rfmf_context* ctx, const rfmf_graph* g, int64_t max_weighted_deg,
+                           int64_t C, const int8_t* initial_spins, const double* t0s,
+                           int64_t nphases, const uint64_t* phases, const uint64_t* iters,
+                           const uint64_t* solver_seeds, const rfmf_launch_config* cfg,
+                           int8_t* end_spins, int8_t* best_spins, float* kernel_ms,
+                           int64_t* kernel_best_vals, int64_t* kernel_final_vals) {
+    try {
+        return rfmf_anneal_impl(ctx, g, max_weighted_deg, C, initial_spins, t0s, nphases, phases, iters, solver_seeds, cfg, end_spins, best_spins, kernel_ms, kernel_best_vals, kernel_final_vals);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_anneal");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_anneal");
+    }
 }

@@ -279,7 +279,7 @@ extern "C" void rfmf_initial_spins(uint64_t seed, int64_t n, int8_t* out) {
     }
 }
 
-extern "C" int rfmf_beta_tables(const double* t0s, int64_t C, int64_t total_steps,
+static int rfmf_beta_tables_impl(const double* t0s, int64_t C, int64_t total_steps,
                                 int64_t* run_end, int32_t* run_val, int64_t* chain_off,
                                 int64_t cap, int64_t* runs) {
     if (C < 0 || (C > 0 && !t0s) || total_steps < 0) return fail(RFMF_ERR_INVALID, "bad arguments");
@@ -344,7 +344,7 @@ int validate_csr(int64_t n, const uint32_t* offsets, const int32_t* col, const i
 }
 }  // namespace
 
-extern "C" int rfmf_csr_validate(int64_t n, const uint32_t* offsets, const int32_t* col,
+static int rfmf_csr_validate_impl(int64_t n, const uint32_t* offsets, const int32_t* col,
                                  const int32_t* weight, int64_t* max_weighted_degree) {
     CsrFacts f;
     const int rc = validate_csr(n, offsets, col, weight, f);
@@ -352,7 +352,7 @@ extern "C" int rfmf_csr_validate(int64_t n, const uint32_t* offsets, const int32
     return rc;
 }
 
-extern "C" int rfmf_graph_create(rfmf_context* ctx, int64_t n, const uint32_t* offsets,
+static int rfmf_graph_create_impl(rfmf_context* ctx, int64_t n, const uint32_t* offsets,
                                  const int32_t* col, const int32_t* weight, rfmf_graph** out) {
     if (!ctx || !out) return fail(RFMF_ERR_INVALID, "ctx/out is NULL");
     *out = nullptr;
@@ -453,3 +453,37 @@ bool compact_key_safe(int64_t total, double t0, int64_t B, int kb) {
 
 }  // namespace rfmf
 
+// C ABI entry points: no C++ exception crosses the boundary.
+extern "C" int rfmf_graph_create(rfmf_context* ctx, int64_t n, const uint32_t* offsets,
+                                 const int32_t* col, const int32_t* weight, rfmf_graph** out) {
+    try {
+        return rfmf_graph_create_impl(ctx, n, offsets, col, weight, out);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_graph_create");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_graph_create");
+    }
+}
+
+extern "C" int rfmf_beta_tables(const double* t0s, int64_t C, int64_t total_steps,
+                                int64_t* run_end, int32_t* run_val, int64_t* chain_off,
+                                int64_t cap, int64_t* runs) {
+    try {
+        return rfmf_beta_tables_impl(t0s, C, total_steps, run_end, run_val, chain_off, cap, runs);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_beta_tables");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_beta_tables");
+    }
+}
+
+extern "C" int rfmf_csr_validate(int64_t n, const uint32_t* offsets, const int32_t* col,
+                                 const int32_t* weight, int64_t* max_weighted_degree) {
+    try {
+        return rfmf_csr_validate_impl(n, offsets, col, weight, max_weighted_degree);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_csr_validate");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_csr_validate");
+    }
+}

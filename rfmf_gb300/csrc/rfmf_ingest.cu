@@ -114,7 +114,7 @@ extern "C" int rfmf_gset_header(const char* text, size_t len, int64_t* n, int64_
     return RFMF_OK;
 }
 
-extern "C" int rfmf_gset_parse(const char* text, size_t len, double forced_scale, int64_t cap,
+static int rfmf_gset_parse_impl(const char* text, size_t len, double forced_scale, int64_t cap,
                                int64_t* u, int64_t* v, int64_t* w, int64_t* nedges,
                                double* scale_out, int64_t* zero_dropped) {
     if (!text || !u || !v || !w || !nedges) return fail(RFMF_ERR_INVALID, "NULL argument");
@@ -414,7 +414,7 @@ unsigned grid_for(int64_t n) {
 
 }  // namespace
 
-extern "C" int rfmf_graph_from_edges(rfmf_context* ctx, int64_t nedges, const int64_t* u,
+static int rfmf_graph_from_edges_impl(rfmf_context* ctx, int64_t nedges, const int64_t* u,
                                      const int64_t* v, const int64_t* w, rfmf_graph** out,
                                      int64_t* n_out) {
     if (!ctx || !out || nedges < 0 || (nedges > 0 && (!u || !v || !w)))
@@ -548,7 +548,7 @@ extern "C" int rfmf_graph_from_edges(rfmf_context* ctx, int64_t nedges, const in
     return RFMF_OK;
 }
 
-extern "C" int rfmf_graph_orig_ids(const rfmf_graph* g, int64_t* out) {
+static int rfmf_graph_orig_ids_impl(const rfmf_graph* g, int64_t* out) {
     if (!g || !out) return fail(RFMF_ERR_INVALID, "graph/out is NULL");
     if (static_cast<int64_t>(g->origIds.size()) != g->n)
         return fail(RFMF_ERR_INVALID, "graph was not built from an edge list");
@@ -556,7 +556,7 @@ extern "C" int rfmf_graph_orig_ids(const rfmf_graph* g, int64_t* out) {
     return RFMF_OK;
 }
 
-extern "C" int rfmf_graph_csr(const rfmf_graph* g, uint32_t* offsets, int32_t* col, int32_t* weight) {
+static int rfmf_graph_csr_impl(const rfmf_graph* g, uint32_t* offsets, int32_t* col, int32_t* weight) {
     if (!g) return fail(RFMF_ERR_INVALID, "graph is NULL");
     CU(cudaSetDevice(g->ctx->device));
     const int64_t m2 = 2 * g->m;
@@ -641,3 +641,48 @@ cudaError_t launch_chain_partitions(const DevChain* chains, const DevGraph* grap
 }
 
 }  // namespace rfmf
+
+// C ABI entry points: no C++ exception crosses the boundary.
+extern "C" int rfmf_gset_parse(const char* text, size_t len, double forced_scale, int64_t cap,
+                               int64_t* u, int64_t* v, int64_t* w, int64_t* nedges,
+                               double* scale_out, int64_t* zero_dropped) {
+    try {
+        return rfmf_gset_parse_impl(text, len, forced_scale, cap, u, v, w, nedges, scale_out, zero_dropped);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_gset_parse");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_gset_parse");
+    }
+}
+
+extern "C" int rfmf_graph_from_edges(rfmf_context* ctx, int64_t nedges, const int64_t* u,
+                                     const int64_t* v, const int64_t* w, rfmf_graph** out,
+                                     int64_t* n_out) {
+    try {
+        return rfmf_graph_from_edges_impl(ctx, nedges, u, v, w, out, n_out);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_graph_from_edges");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_graph_from_edges");
+    }
+}
+
+extern "C" int rfmf_graph_csr(const rfmf_graph* g, uint32_t* offsets, int32_t* col, int32_t* weight) {
+    try {
+        return rfmf_graph_csr_impl(g, offsets, col, weight);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_graph_csr");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_graph_csr");
+    }
+}
+
+extern "C" int rfmf_graph_orig_ids(const rfmf_graph* g, int64_t* out) {
+    try {
+        return rfmf_graph_orig_ids_impl(g, out);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_graph_orig_ids");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_graph_orig_ids");
+    }
+}

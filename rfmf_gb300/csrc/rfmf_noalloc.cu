@@ -28,6 +28,7 @@
 #include <cstring>
 #include <limits>
 #include <mutex>
+#include <new>
 #include <vector>
 
 #include "../../include/rfmf.h"
@@ -113,7 +114,7 @@ cudaError_t noalloc_wsum(const int32_t* edges, int64_t m2, int64_t* out, cudaStr
 
 }  // namespace
 
-extern "C" int rfmf_anneal_noalloc(int device, void* stream, int64_t n,
+static int rfmf_anneal_noalloc_impl(int device, void* stream, int64_t n,
                                    const uint32_t* d_offsets, const int32_t* d_edges,
                                    int64_t max_weighted_deg, int64_t C, const double* t0s,
                                    const uint64_t* solver_seeds, int64_t nphases,
@@ -301,3 +302,21 @@ extern "C" int rfmf_anneal_noalloc(int device, void* stream, int64_t n,
     return RFMF_OK;
 }
 
+// C ABI entry points: no C++ exception crosses the boundary.
+extern "C" int rfmf_anneal_noalloc(int device, void* stream, int64_t n,
+                                   const uint32_t* d_offsets, const int32_t* d_edges,
+                                   int64_t max_weighted_deg, int64_t C, const double* t0s,
+                                   const uint64_t* solver_seeds, int64_t nphases,
+                                   const uint64_t* phases, const uint64_t* iters,
+                                   const int64_t* d_beta_end, const int32_t* d_beta_val,
+                                   const int64_t* chain_beta_off, const int64_t* chain_beta_runs,
+                                   uint32_t* d_spin_bits, uint32_t* d_best_bits,
+                                   int64_t* d_cur, int64_t* d_best) {
+    try {
+        return rfmf_anneal_noalloc_impl(device, stream, n, d_offsets, d_edges, max_weighted_deg, C, t0s, solver_seeds, nphases, phases, iters, d_beta_end, d_beta_val, chain_beta_off, chain_beta_runs, d_spin_bits, d_best_bits, d_cur, d_best);
+    } catch (const std::bad_alloc&) {
+        return rfmf::set_last_error(RFMF_ERR_NOMEM, "host allocation failed in rfmf_anneal_noalloc");
+    } catch (...) {
+        return rfmf::set_last_error(RFMF_ERR_INVALID, "unexpected host exception in rfmf_anneal_noalloc");
+    }
+}

@@ -464,8 +464,31 @@ void fail_request(Request& r, int code, const std::string& msg, double t) {
     r.finishS = t;
 }
 
+void worker_loop(rfmf_server* s);
+
+// The worker: any host exception (allocation failure) fails the requests it
+// holds instead of terminating the process.
 void worker_main(rfmf_server* s) {
     cudaSetDevice(s->ctx->device);
+    for (;;) {
+        try {
+            worker_loop(s);
+            return;
+        } catch (...) {
+            std::lock_guard<std::mutex> lk(s->mu);
+            const double t = s->now();
+            for (ReqPtr& r : s->running) {
+                fail_request(*r, RFMF_ERR_NOMEM, "host allocation failed in the server worker", t);
+                release(s, *r);
+            }
+            s->running.clear();
+            s->runningChains = 0;
+            s->cvDone.notify_all();
+        }
+    }
+}
+
+void worker_loop(rfmf_server* s) {
     for (;;) {
         std::vector<ReqPtr> admitNow;
         {
@@ -566,7 +589,7 @@ rfmf_request_status status_of(const Request& r) {
 
 }  // namespace
 
-extern "C" int rfmf_server_create(rfmf_context* ctx, const rfmf_server_config* cfg, rfmf_server** out) {
+static int rfmf_server_create_impl(rfmf_context* ctx, const rfmf_server_config* cfg, rfmf_server** out) {
     if (!ctx || !out) return fail(RFMF_ERR_INVALID, "ctx/out is NULL");
     *out = nullptr;
     auto s = std::unique_ptr<rfmf_server>(new (std::nothrow) rfmf_server());
@@ -620,7 +643,7 @@ extern "C" int rfmf_server_destroy(rfmf_server* s) {
     return RFMF_OK;
 }
 
-extern "C" int rfmf_submit(rfmf_server* s, const rfmf_graph* g, int64_t nchains,
+static int rfmf_submit_impl(rfmf_server* s, const rfmf_graph* g, int64_t nchains,
                            const int8_t* initial_spins, const double* t0s, int64_t nphases,
                            const uint64_t* phases, const uint64_t* iters,
                            const uint64_t* solver_seeds, uint64_t* request_id) {
@@ -674,14 +697,16 @@ extern "C" int rfmf_submit(rfmf_server* s, const rfmf_graph* g, int64_t nchains,
     else if (c.csr_format == 1) { if (!g->unit16) return fail(RFMF_ERR_INVALID, "unit16 CSR needs |w| == 1 and n <= 32768"); fmt = kCsrUnit16; }
     else if (c.csr_format == 2) { if (!g->packed32) return fail(RFMF_ERR_INVALID, "packed32 CSR needs |w| < 2^15 and n <= 65536"); fmt = kCsrPacked32; }
     else fmt = kCsrGlobal;
-    // One chain beside the shared CSR must fit a CTA, else walk the CSR in HBM.
+    // The shared CSR must leave room for about 8 warps of chains per CTA (or
+    // the request's chains, if fewer), else the CSR is walked in HBM.
     {
         cudaFuncAttributes fa{};
         CU(cudaFuncGetAttributes(&fa, kernel_ptr(r->dbytes, fmt, r->s64)));
         const int64_t dynMax = s->ctx->smemOptin - static_cast<int64_t>(fa.sharedSizeBytes);
         const uint32_t chainB = chain_layout(static_cast<int>(g->n), static_cast<int>(r->words), r->pmax,
                                              r->W, r->dbytes).total;
-        if (fmt != kCsrGlobal && static_cast<int64_t>(kSmemHeader) + csr_bytes(g, fmt) + chainB > dynMax) {
+        const int64_t kWant = std::min<int64_t>(nchains, std::max(1, 8 / r->W));
+        if (fmt != kCsrGlobal && static_cast<int64_t>(kSmemHeader) + csr_bytes(g, fmt) + kWant * chainB > dynMax) {
             if (c.csr_format != 0) return fail(RFMF_ERR_CAPACITY, "the shared-memory CSR does not fit");
             fmt = kCsrGlobal;
         }
@@ -709,7 +734,7 @@ extern "C" int rfmf_submit(rfmf_server* s, const rfmf_graph* g, int64_t nchains,
     return RFMF_OK;
 }
 
-extern "C" int rfmf_poll(rfmf_server* s, uint64_t request_id, rfmf_request_status* status) {
+static int rfmf_poll_impl(rfmf_server* s, uint64_t request_id, rfmf_request_status* status) {
     if (!s || !status) return fail(RFMF_ERR_INVALID, "server/status is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->all.find(request_id);
@@ -718,7 +743,7 @@ extern "C" int rfmf_poll(rfmf_server* s, uint64_t request_id, rfmf_request_statu
     return RFMF_OK;
 }
 
-extern "C" int rfmf_wait(rfmf_server* s, uint64_t request_id, double timeout_s,
+static int rfmf_wait_impl(rfmf_server* s, uint64_t request_id, double timeout_s,
                          rfmf_request_status* status) {
     if (!s) return fail(RFMF_ERR_INVALID, "server is NULL");
     std::unique_lock<std::mutex> lk(s->mu);
@@ -737,7 +762,7 @@ extern "C" int rfmf_wait(rfmf_server* s, uint64_t request_id, double timeout_s,
     return RFMF_OK;
 }
 
-extern "C" int rfmf_result(rfmf_server* s, uint64_t request_id, int8_t* end_spins, int8_t* best_spins,
+static int rfmf_result_impl(rfmf_server* s, uint64_t request_id, int8_t* end_spins, int8_t* best_spins,
                            int64_t* best_vals, int64_t* final_vals) {
     if (!s) return fail(RFMF_ERR_INVALID, "server is NULL");
     ReqPtr r;
@@ -767,7 +792,7 @@ extern "C" int rfmf_result(rfmf_server* s, uint64_t request_id, int8_t* end_spin
     return RFMF_OK;
 }
 
-extern "C" int rfmf_server_stats_get(rfmf_server* s, rfmf_server_stats* out) {
+static int rfmf_server_stats_get_impl(rfmf_server* s, rfmf_server_stats* out) {
     if (!s || !out) return fail(RFMF_ERR_INVALID, "server/out is NULL");
     std::lock_guard<std::mutex> lk(s->mu);
     *out = s->stats;
@@ -779,4 +804,70 @@ extern "C" int rfmf_server_stats_get(rfmf_server* s, rfmf_server_stats* out) {
         else ++out->done;
     }
     return RFMF_OK;
+}
+
+// C ABI entry points: no C++ exception crosses the boundary.
+extern "C" int rfmf_server_create(rfmf_context* ctx, const rfmf_server_config* cfg, rfmf_server** out) {
+    try {
+        return rfmf_server_create_impl(ctx, cfg, out);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_server_create");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_server_create");
+    }
+}
+
+extern "C" int rfmf_submit(rfmf_server* s, const rfmf_graph* g, int64_t nchains,
+                           const int8_t* initial_spins, const double* t0s, int64_t nphases,
+                           const uint64_t* phases, const uint64_t* iters,
+                           const uint64_t* solver_seeds, uint64_t* request_id) {
+    try {
+        return rfmf_submit_impl(s, g, nchains, initial_spins, t0s, nphases, phases, iters, solver_seeds, request_id);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_submit");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_submit");
+    }
+}
+
+extern "C" int rfmf_wait(rfmf_server* s, uint64_t request_id, double timeout_s,
+                         rfmf_request_status* status) {
+    try {
+        return rfmf_wait_impl(s, request_id, timeout_s, status);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_wait");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_wait");
+    }
+}
+
+extern "C" int rfmf_result(rfmf_server* s, uint64_t request_id, int8_t* end_spins, int8_t* best_spins,
+                           int64_t* best_vals, int64_t* final_vals) {
+    try {
+        return rfmf_result_impl(s, request_id, end_spins, best_spins, best_vals, final_vals);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_result");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_result");
+    }
+}
+
+extern "C" int rfmf_poll(rfmf_server* s, uint64_t request_id, rfmf_request_status* status) {
+    try {
+        return rfmf_poll_impl(s, request_id, status);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_poll");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_poll");
+    }
+}
+
+extern "C" int rfmf_server_stats_get(rfmf_server* s, rfmf_server_stats* out) {
+    try {
+        return rfmf_server_stats_get_impl(s, out);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_server_stats_get");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_server_stats_get");
+    }
 }

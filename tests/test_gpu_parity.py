@@ -182,6 +182,31 @@ def test_multi_graph_batch_isolation(rfmf, ctx, oracle):
         assert out["cur_vals"][i] == o["cur_vals"][0]
 
 
+def test_isolation_across_waves_and_determinism(rfmf, ctx):
+    """Chain isolation and determinism (tests/test_chain_isolation.sh): 3000
+    chains at one chain per CTA are more work items than the GPU holds
+    resident (16 CTAs per SM x 152 SMs), so items run in waves; every chain
+    equals its C = 1 run, and the same launch repeated gives the same bytes."""
+    g = rfmf.erdos_renyi(400, 0.03, signed=True, seed=21)
+    dg = rfmf.DeviceGraph(ctx, g)
+    from conftest import chains_for
+    seeds = list(range(3000))
+    init, solver = chains_for(g, seeds)
+    t0s = [FULL_LADDER[i % 8] for i in range(3000)]
+    phases, iters = [16, 4, 1], [60, 60, 60]
+    cfg = rfmf.make_config(chains_per_cta=1)
+    a = rfmf.anneal_gpu(ctx, dg, g.max_weighted_degree(), init, t0s, phases, iters, solver, cfg)
+    b = rfmf.anneal_gpu(ctx, dg, g.max_weighted_degree(), init, t0s, phases, iters, solver, cfg)
+    assert np.array_equal(a.end_spins, b.end_spins) and np.array_equal(a.best_spins, b.best_spins)
+    assert np.array_equal(a.best_vals, b.best_vals) and np.array_equal(a.final_vals, b.final_vals)
+    for i in (0, 1, 1499, 2999):
+        one = rfmf.anneal_gpu(ctx, dg, g.max_weighted_degree(), init[i:i + 1], [t0s[i]], phases,
+                              iters, [solver[i]])
+        assert np.array_equal(one.end_spins[0], a.end_spins[i]), i
+        assert np.array_equal(one.best_spins[0], a.best_spins[i]), i
+        assert one.best_vals[0] == a.best_vals[i] and one.final_vals[0] == a.final_vals[i]
+
+
 def test_cuda_graph_replay(rfmf, ctx, oracle):
     g = rfmf.erdos_renyi_degree(500, 8, signed=True, seed=9)
     seeds = [11, 12, 13, 14]
