@@ -161,7 +161,7 @@ typedef struct rfmf_launch_config {
     int corr;              /* CorrMode; accepted, no effect (FLIP needs no corr walk) */
     int device;            /* informational; the context's device is used */
     int s_width;           /* 32 or 64; accepted (the per-vertex gain width is gain_width) */
-    int threads_per_chain; /* 0 = auto, else 32, 64 or 128 (one chain's warp group) */
+    int threads_per_chain; /* 0 = auto, else 32, 64, 128 or 256 (one chain's warp group) */
     int score_path;        /* 0 = gate (src/host_common.cpp:296-312), 1 = int32, 2 = int64 */
     int chains_per_cta;    /* 0 = auto, else chains sharing one CTA's copy of the graph */
     int csr_format;        /* 0 = auto, 1 = unit16 (shared), 2 = packed32 (shared), 3 = HBM */

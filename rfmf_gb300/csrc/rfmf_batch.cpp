@@ -321,8 +321,8 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
     rfmf_launch_config dflt{};
     const rfmf_launch_config& c = cfg ? *cfg : dflt;
     if (c.threads_per_chain && c.threads_per_chain != 32 && c.threads_per_chain != 64 &&
-        c.threads_per_chain != 128)
-        return fail(RFMF_ERR_INVALID, "threads_per_chain must be 0, 32, 64 or 128");
+        c.threads_per_chain != 128 && c.threads_per_chain != 256)
+        return fail(RFMF_ERR_INVALID, "threads_per_chain must be 0, 32, 64, 128 or 256");
     if (c.gain_width != 0 && c.gain_width != 1 && c.gain_width != 4)
         return fail(RFMF_ERR_INVALID, "gain_width must be 0, 1 or 4");
     if (c.csr_format < 0 || c.csr_format > 3) return fail(RFMF_ERR_INVALID, "csr_format must be 0..3");
@@ -375,7 +375,7 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
         const int dbytes = c.gain_width ? c.gain_width : (g->B <= 127 ? 1 : 4);
         if (dbytes == 1 && g->B > 127)
             return fail(RFMF_ERR_INVALID, "int8 gains need max weighted degree <= 127 (B=%lld)", (long long)g->B);
-        const int W = choose_warps(static_cast<int>(g->n), c);
+        const int W = choose_warps(static_cast<int>(g->n), c, b->C, ctx->sms);
         bool s64 = (c.score_path == 2);
         if (!s64) {
             for (int32_t ch : chainsOfGraph[gi])

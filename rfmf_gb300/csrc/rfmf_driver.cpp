@@ -425,11 +425,20 @@ extern "C" int rfmf_graph_info(const rfmf_graph* g, int64_t* n, int64_t* m, int6
 namespace rfmf {
 // Warps per chain: one unless a chain has enough vertex blocks to keep more
 // warps busy (about 384 blocks of 8 vertices per extra warp).
-int choose_warps(int maxN, const rfmf_launch_config& c) {
+int choose_warps(int maxN, const rfmf_launch_config& c, int64_t chains, int sms) {
     if (c.threads_per_chain) return c.threads_per_chain / 32;
     int W = 1;
     const int nblk = (maxN + 7) / 8;
+    // About 768 vertex blocks per warp.
     while (W < 4 && nblk >= 384 * 2 * W) W *= 2;
+    // Too few chains to fill the SMs: widen each chain while all chains stay
+    // within 8 warps per SM and the current width still has a vertex block
+    // per thread.  One warp per chain is the most efficient form once chains
+    // alone fill the SMs; below that, per-chain latency is what the extra
+    // warps buy (GB300, 256 chains of ER n = 2000: 67.5 -> 88.6 M
+    // chain-steps/s from one warp to four; 32 chains of ER n = 800: 6.7 -> 11.0).
+    while (W < kMaxAutoWarps && chains > 0 && chains * 2 * W <= int64_t(8) * sms && nblk >= 32 * W)
+        W *= 2;
     return W;
 }
 

@@ -58,7 +58,10 @@ int build_beta(const double* t0s, int64_t C, int64_t total, BetaTables& bt);
 bool score_safe_int32(int64_t total, double t0, int64_t B);
 
 // Launch-shape helpers of the planner.
-int choose_warps(int maxN, const rfmf_launch_config& c);
+// Warps per chain: at least one per ~768 vertex blocks, more while the batch's
+// `chains` leave the SMs (`sms`) short of work; c.threads_per_chain overrides.
+constexpr int kMaxAutoWarps = 4;
+int choose_warps(int maxN, const rfmf_launch_config& c, int64_t chains, int sms);
 int key_bits(int64_t n, int T);
 bool compact_key_safe(int64_t total, double t0, int64_t B, int kb);
 

@@ -603,8 +603,8 @@ static int rfmf_server_create_impl(rfmf_context* ctx, const rfmf_server_config* 
     }
     const rfmf_launch_config& c = s->lc;
     if (c.threads_per_chain && c.threads_per_chain != 32 && c.threads_per_chain != 64 &&
-        c.threads_per_chain != 128)
-        return fail(RFMF_ERR_INVALID, "threads_per_chain must be 0, 32, 64 or 128");
+        c.threads_per_chain != 128 && c.threads_per_chain != 256)
+        return fail(RFMF_ERR_INVALID, "threads_per_chain must be 0, 32, 64, 128 or 256");
     if (c.gain_width != 0 && c.gain_width != 1 && c.gain_width != 4)
         return fail(RFMF_ERR_INVALID, "gain_width must be 0, 1 or 4");
     if (c.csr_format < 0 || c.csr_format > 3) return fail(RFMF_ERR_INVALID, "csr_format must be 0..3");
@@ -683,7 +683,15 @@ static int rfmf_submit_impl(rfmf_server* s, const rfmf_graph* g, int64_t nchains
     if (r->dbytes == 1 && g->B > 127)
         return fail(RFMF_ERR_INVALID, "int8 gains need max weighted degree <= 127 (B=%lld)",
                     static_cast<long long>(g->B));
-    r->W = choose_warps(static_cast<int>(g->n), c);
+    // Warps per chain from the load at submission: the chains running and
+    // queued, plus this request's.
+    int64_t load = nchains;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        load += s->runningChains;
+        for (const ReqPtr& q : s->queue) load += q->C;
+    }
+    r->W = choose_warps(static_cast<int>(g->n), c, load, s->ctx->sms);
     r->s64 = (c.score_path == 2);
     if (!r->s64) {
         for (int64_t k = 0; k < nchains && !r->s64; ++k)

@@ -64,3 +64,20 @@ def test_multi_class_batch_matches_standalone(rfmf, ctx, use_graph):
         assert np.array_equal(np.stack(r["end_spins"][sl]), ref.end_spins), k
         assert np.array_equal(r["best_vals"][sl], ref.best_vals), k
         assert np.array_equal(r["cur_vals"][sl], ref.final_vals), k
+
+
+def test_auto_warps_follow_chain_count(rfmf, ctx):
+    """Few chains per SM get wider warp groups; enough chains to fill the SMs
+    run one warp each.  Results do not depend on the width (covered by the
+    schedule-invariance knobs); this checks the plan."""
+    g = rfmf.erdos_renyi(800, 0.06, seed=0)
+    dg = rfmf.DeviceGraph(ctx, g)
+    sms = ctx.info()["sm_count"]
+    widths = {}
+    for C in (32, 8 * sms):
+        init, solver = chains_for(g, list(range(C)))
+        b = rfmf.Batch(ctx, [dg] * C, [70.0] * C, solver, list(init), [8, 1], [4, 4])
+        widths[C] = b.info()["threads_per_chain"]
+        b.close()
+    assert widths[32] > 32, widths
+    assert widths[8 * sms] == 32, widths

@@ -65,9 +65,10 @@ def test_small_graphs_phases(rfmf, ctx, oracle, phases):
 
 
 KNOBS = ([dict(csr_format=f, gain_width=w) for f in (1, 2, 3) for w in (1, 4)] +
-         [dict(threads_per_chain=t) for t in (64, 128)] +
+         [dict(threads_per_chain=t) for t in (64, 128, 256)] +
          [dict(chains_per_cta=k) for k in (1, 5)] +
-         [dict(threads_per_chain=64, chains_per_cta=3, csr_format=3, gain_width=1)])
+         [dict(threads_per_chain=64, chains_per_cta=3, csr_format=3, gain_width=1),
+          dict(threads_per_chain=256, chains_per_cta=2, csr_format=2, gain_width=4)])
 
 
 @pytest.mark.parametrize("knobs", KNOBS, ids=lambda k: ",".join(f"{a}={b}" for a, b in k.items()))
