@@ -431,6 +431,76 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
         k.graphs.push_back(static_cast<int>(gi));
         k.chainsOf.push_back(chainsOfGraph[gi]);
     }
+    // A shared-memory class's CTA holds the class's largest CSR beside K
+    // chains sized for its largest graph.  While that leaves room for fewer
+    // chains than a CTA should hold (as above, over the class), the graph
+    // demanding the most moves to the HBM class of the same key, so that a
+    // few large graphs do not shrink every CTA of the class.
+    if (c.csr_format == 0) {
+        const int64_t perSm = (b->C + ctx->sms - 1) / std::max(ctx->sms, 1);
+        for (size_t ci = 0; ci < b->cls.size(); ++ci) {
+            if (b->cls[ci].fmt == kCsrGlobal) continue;
+            cudaFuncAttributes fa{};
+            const int64_t dynMax =
+                dyn_smem_max(ctx, kernel_ptr(b->cls[ci].dbytes, b->cls[ci].fmt, b->cls[ci].score64), fa);
+            while (!b->cls[ci].graphs.empty()) {
+                BatchClass& k = b->cls[ci];
+                auto chainOf = [&](int64_t n) {
+                    const int ni = static_cast<int>(n);
+                    return static_cast<int64_t>(
+                        chain_layout(ni, (ni + 31) / 32, std::max(1, std::min(k.pmax, ni)), k.warps, k.dbytes).total);
+                };
+                int64_t maxN = 0, maxCsr = 0, maxCh = 0;
+                for (size_t q = 0; q < k.graphs.size(); ++q) {
+                    const rfmf_graph* g = b->glist[k.graphs[q]];
+                    maxN = std::max(maxN, g->n);
+                    maxCsr = std::max<int64_t>(maxCsr, csr_bytes(g, k.fmt));
+                    maxCh = std::max<int64_t>(maxCh, static_cast<int64_t>(k.chainsOf[q].size()));
+                }
+                const int64_t kWant =
+                    std::max<int64_t>(1, std::min<int64_t>({maxCh, static_cast<int64_t>(std::max(1, 8 / k.warps)), perSm}));
+                if (dynMax > 0 && static_cast<int64_t>(kSmemHeader) + maxCsr + kWant * chainOf(maxN) <= dynMax) break;
+                size_t worst = 0;
+                int64_t worstD = -1;
+                for (size_t q = 0; q < k.graphs.size(); ++q) {
+                    const rfmf_graph* g = b->glist[k.graphs[q]];
+                    const int64_t d = static_cast<int64_t>(csr_bytes(g, k.fmt)) + kWant * chainOf(g->n);
+                    if (d > worstD) { worstD = d; worst = q; }
+                }
+                const int gi = k.graphs[worst];
+                std::vector<int32_t> chains = std::move(k.chainsOf[worst]);
+                k.graphs.erase(k.graphs.begin() + static_cast<std::ptrdiff_t>(worst));
+                k.chainsOf.erase(k.chainsOf.begin() + static_cast<std::ptrdiff_t>(worst));
+                const int dbytes = k.dbytes, W = k.warps, pmax = k.pmax;
+                const bool s64 = k.score64;
+                const Key gk{dbytes, kCsrGlobal, W, s64 ? 1 : 0};
+                auto it = classOf.find(gk);
+                if (it == classOf.end()) {
+                    it = classOf.emplace(gk, static_cast<int>(b->cls.size())).first;
+                    b->cls.emplace_back();     // invalidates k
+                    BatchClass& h = b->cls.back();
+                    h.dbytes = dbytes;
+                    h.fmt = kCsrGlobal;
+                    h.warps = W;
+                    h.score64 = s64;
+                    h.pmax = pmax;
+                }
+                b->cls[it->second].graphs.push_back(gi);
+                b->cls[it->second].chainsOf.push_back(std::move(chains));
+                graphClass[gi] = it->second;
+            }
+        }
+        // Drop classes emptied by the moves and renumber.
+        std::vector<int> remap(b->cls.size(), -1);
+        std::vector<BatchClass> kept;
+        for (size_t ci = 0; ci < b->cls.size(); ++ci) {
+            if (b->cls[ci].graphs.empty()) continue;
+            remap[ci] = static_cast<int>(kept.size());
+            kept.push_back(std::move(b->cls[ci]));
+        }
+        b->cls = std::move(kept);
+        for (size_t gi = 0; gi < G; ++gi) graphClass[gi] = remap[graphClass[gi]];
+    }
     const bool exact = b->cls.size() > 1;
     for (BatchClass& k : b->cls) {
         int rc = plan_class(*b, k, c, exact);
