@@ -108,13 +108,21 @@ class ClockSampler:
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         self.p = None
 
-    def start(self):
+    def start(self, first_sample_timeout=30.0):
+        """Start sampling and return once the first sample is written (NVML
+        is initialised), so the sampler's start-up stays out of timed work."""
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
                                        "--format=csv,noheader,nounits", "-lms", "200"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
+            return
+        t_end = time.perf_counter() + first_sample_timeout
+        while time.perf_counter() < t_end and self.p.poll() is None:
+            if os.path.getsize(self.f.name) > 0:
+                break
+            time.sleep(0.05)
 
     def stop(self):
         if self.p:
@@ -280,7 +288,7 @@ def gpu_arm(args, rank, world):
         dist.barrier()
     torch.cuda.synchronize()
     clocks.start()
-    time.sleep(1.0)   # let the sampler's first NVML queries finish before the timed region
+    time.sleep(0.5)
     t_wall = time.perf_counter()
     step_ms, step_bytes, best_by_step = [], [], []
     imp_prev = np.zeros(len(graphs) * args.chains, np.uint64)
@@ -407,6 +415,7 @@ def gpu_arm(args, rank, world):
             "bytes_model": "5n + min(P,n)(8 + 16 dbar) per chain-sweep + n per improving sweep",
         },
         "wall_s": wall,
+        "step_ms": [round(m, 3) for m in step_ms],
     }
     return result
 
