@@ -700,7 +700,7 @@ def main():
     ap.add_argument("--batched-graphs", type=int, default=512)
     ap.add_argument("--batched-sweeps", type=int, default=2000)
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--serve-rate", default="2", help="req/s; a comma list sweeps several rates")
+    ap.add_argument("--serve-rate", default="2,10", help="req/s; a comma list sweeps several rates")
     ap.add_argument("--serve-seconds", type=float, default=20.0)
     ap.add_argument("--serve-sweeps", type=int, default=100_000)
     ap.add_argument("--serve-window", type=int, default=4096)
