@@ -531,6 +531,43 @@ __device__ __forceinline__ void flip_winner(const ChainSmem& s, int g, int v, Lo
     }
 }
 
+// FLIP step 2 of a one-warp chain at P >= 64 with +-1 weights in the 16-bit
+// CSR (entry = col << 1 | w < 0) and int8 gains: one lane per winner row,
+// four entries in flight.  With spins as bits (1 = +1), D[col] changes by +2
+// when s_b, s_col and the weight bit XOR to 0, else by -2, added into byte
+// lane col & 3 of word col >> 2 (the biased bytes never carry, see D8).
+// (At smaller P the generic walk, which spreads a row over several lanes,
+// is faster.)
+__device__ __forceinline__ void flip2_unit16_d8_warp(const ChainSmem& s, const CsrView& csr, int P, int lane) {
+    const uint16_t* ent = static_cast<const uint16_t*>(csr.ent);
+    unsigned int* Dw = reinterpret_cast<unsigned int*>(s.D);
+    const unsigned char* sb = s.sb;
+    for (int gi = lane; gi < P; gi += 32) {
+        const int v = s.win[gi];
+        if (v < 0) continue;
+        const uint32_t sv = sb[v];
+        uint32_t i = csr.off[v];
+        const uint32_t hi = csr.off[v + 1];
+        for (; i + 4 <= hi; i += 4) {
+            uint32_t e[4], sx[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) e[j] = ent[i + j];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) sx[j] = sb[e[j] >> 1];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint32_t neg = (sv ^ sx[j] ^ e[j]) & 1u;
+                atomicAdd(Dw + (e[j] >> 3), (neg ? 0xFFFFFFFEu : 2u) << ((e[j] & 6u) << 2));
+            }
+        }
+        for (; i < hi; ++i) {
+            const uint32_t e0 = ent[i];
+            const uint32_t neg = (sv ^ sb[e0 >> 1] ^ e0) & 1u;
+            atomicAdd(Dw + (e0 >> 3), (neg ? 0xFFFFFFFEu : 2u) << ((e0 & 6u) << 2));
+        }
+    }
+}
+
 // How select32 hands its winners to FLIP step 1.
 enum WinnerHandoff : int {
     kWinSlots = 0,      // packed keys in the group slots (any warp count, any P)
@@ -946,7 +983,9 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
 
         // ---- FLIP 2: D[x] += 2 w s_b s_x over the winners' rows (new spins);
         // `lanes` consecutive threads share a row, four entries in flight.
-        {
+        if (kFmt == kCsrUnit16 && std::is_same<DP, D8>::value && T == 32 && P >= 64) {
+            flip2_unit16_d8_warp(s, csr, P, t);
+        } else {
             const int lanes = 1 << pc.laneShift;
             const int sub = t & (lanes - 1);
             for (int gi = t >> pc.laneShift; gi < P; gi += T >> pc.laneShift) {
