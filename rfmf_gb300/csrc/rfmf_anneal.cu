@@ -20,7 +20,7 @@
 //     the best-so-far spins as bits.  Graphs too big for shared memory walk
 //     their CSR in HBM instead (kCsrGlobal); the chain state stays resident.
 //   * SELECT reads only D.  The sweep-uniform part of the Philox counter is
-//     hoisted (rounds 1-3 lose 3 multiplies and 3 xors per block) and two
+//     hoisted (rounds 1-3 lose 3 multiplies and 3 xors per block) and three
 //     vertex blocks are in flight per thread.
 //   * The group argmax keeps eight register accumulators per thread (one per
 //     Philox lane j) whenever every thread's lane j lands in one group, folds
@@ -490,16 +490,26 @@ __device__ __forceinline__ void score_blocks(int32_t acc[8], const ChainSmem& s,
     int32_t d[NB][8];
 #pragma unroll
     for (int q = 0; q < NB; ++q) philox_block(static_cast<uint32_t>(b + q * T), sc, keys, x[q]);
+    if constexpr (NB >= 3) {
+        // Three blocks' Philox words in flight; each block's gains are
+        // loaded just before it is scored so that they fit the registers.
 #pragma unroll
-    for (int q = 0; q < NB; ++q) DP::load8raw(s.D, b + q * T, d[q]);
+        for (int q = 0; q < NB; ++q) {
+            DP::load8raw(s.D, b + q * T, d[0]);
+            score8_key<kMasked, kF0>(acc, x[q], d[0], betaK, tkb - q, kc, lim);
+        }
+    } else {
 #pragma unroll
-    for (int q = 0; q < NB; ++q) score8_key<kMasked, kF0>(acc, x[q], d[q], betaK, tkb - q, kc, lim);
+        for (int q = 0; q < NB; ++q) DP::load8raw(s.D, b + q * T, d[q]);
+#pragma unroll
+        for (int q = 0; q < NB; ++q) score8_key<kMasked, kF0>(acc, x[q], d[q], betaK, tkb - q, kc, lim);
+    }
 }
 
 // The block loop of select32 (trip counts uniform per warp: its blocks at
 // step k are wb + kT .. wb + kT + 31, so the table shuffles run converged):
-// two blocks in flight while the whole warp has two full blocks left, then a
-// clamped, masked single-block tail.
+// three blocks in flight while the whole warp has three full blocks left,
+// then two, then a clamped, masked single-block tail.
 template <bool kF0, class DP>
 __device__ __forceinline__ void select_blocks(int32_t acc[8], const ChainSmem& s, const SweepConst& sc,
                                               const ChainKeys& keys, int n, int t, int T,
@@ -508,6 +518,8 @@ __device__ __forceinline__ void select_blocks(int32_t acc[8], const ChainSmem& s
     const int nblk = (n + 7) >> 3;
     const int wb = t & ~31;
     int b = t, k = 0;
+    for (; wb + 2 * T + 31 < nfull - k * T; b += 3 * T, k += 3)
+        score_blocks<3, false, kF0, DP>(acc, s, sc, keys, b, T, betaK, tkBase - k, kc, 8);
     for (; wb + T + 31 < nfull - k * T; b += 2 * T, k += 2)
         score_blocks<2, false, kF0, DP>(acc, s, sc, keys, b, T, betaK, tkBase - k, kc, 8);
     for (; wb + k * T < nblk; b += T, ++k) {
