@@ -414,10 +414,26 @@ def gpu_arm(args, rank, world):
                            "during the timed region)",
             "bytes_model": "5n + min(P,n)(8 + 16 dbar) per chain-sweep + n per improving sweep",
         },
+        "issue_roofline": issue_roofline(traffic, value, sm_count, sm_mhz),
         "wall_s": wall,
         "step_ms": [round(m, 3) for m in step_ms],
     }
     return result
+
+
+def issue_roofline(traffic, value, sm_count, sm_mhz):
+    """The bound this integer kernel actually meets: warp instructions per
+    chain-sweep (ncu, same kernel and workload, from the profile summary)
+    times chain-steps/s, against 4 issue slots per SM per cycle."""
+    ipc = (traffic or {}).get("warp_inst_per_chain_sweep")
+    if not ipc:
+        return None
+    achieved = value * ipc / 1e12
+    peak = sm_count * 4.0 * sm_mhz * 1e6 / 1e12
+    return {"bound": "integer issue", "achieved": achieved, "peak": peak, "unit": "T warp-inst/s",
+            "frac": achieved / peak, "warp_inst_per_chain_sweep": ipc,
+            "source": "profiles/anneal_kernel_traffic.json (ncu smsp__inst_executed.sum / chain-sweeps)",
+            "peak_source": f"{sm_count} SMs x 4 warp-inst/clk x {sm_mhz:.0f} MHz"}
 
 
 def plain_kernel_arm(graphs, setup, sweeps, ctx):
