@@ -514,7 +514,7 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
 
     // Beta tables over the executed sweeps.
     BetaTables bt;
-    int rc = build_beta(t0s, C, static_cast<int64_t>(total), bt);
+    int rc = build_beta_cached(ctx, t0s, C, static_cast<int64_t>(total), bt);
     if (rc) return rc;
 
     std::vector<DevGraph> hg(G);

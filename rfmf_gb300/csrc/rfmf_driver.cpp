@@ -123,7 +123,7 @@ int append_runs(double t0, int64_t total, std::vector<int64_t>& end, std::vector
     }
 }
 
-int build_beta(const double* t0s, int64_t C, int64_t total, BetaTables& bt) {
+int beta_range_check(const double* t0s, int64_t C, int64_t total) {
     // beta_fixed must stay inside int32: past it the reference's
     // static_cast<int32_t>(round(...)) (src/host_common.h:73-76) is undefined
     // behaviour (x86 and Arm even disagree), so such schedules are refused.
@@ -134,6 +134,11 @@ int build_beta(const double* t0s, int64_t C, int64_t total, BetaTables& bt) {
                         "t0=%g over %lld sweeps makes beta_fixed overflow int32", t0s[c],
                         static_cast<long long>(total));
     }
+    return RFMF_OK;
+}
+
+int build_beta(const double* t0s, int64_t C, int64_t total, BetaTables& bt) {
+    if (int rc = beta_range_check(t0s, C, total)) return rc;
     std::vector<double> distinct;
     std::vector<int64_t> first, count;
     bt.chainOff.resize(C);
@@ -150,6 +155,66 @@ int build_beta(const double* t0s, int64_t C, int64_t total, BetaTables& bt) {
         }
         bt.chainOff[c] = first[k];
         bt.chainRuns[c] = count[k];
+    }
+    return RFMF_OK;
+}
+
+namespace {
+
+// The run table of one (t0, sweeps): from the context's cache, or built on
+// the calling thread and added.
+int cached_runs(rfmf_context* ctx, double t0, int64_t total, std::shared_ptr<const BetaRun>& out) {
+    uint64_t bits;
+    std::memcpy(&bits, &t0, sizeof bits);
+    const auto key = std::make_pair(bits, static_cast<uint64_t>(total));
+    {
+        std::lock_guard<std::mutex> lk(ctx->betaMu);
+        auto it = ctx->betaCache.find(key);
+        if (it != ctx->betaCache.end()) {
+            out = it->second;
+            return RFMF_OK;
+        }
+    }
+    auto tb = std::make_shared<BetaRun>();
+    if (int rc = append_runs(t0, total, tb->end, tb->val)) return rc;
+    std::lock_guard<std::mutex> lk(ctx->betaMu);
+    if (ctx->betaCachedRuns + static_cast<int64_t>(tb->end.size()) > kBetaCacheRuns) {
+        ctx->betaCache.clear();
+        ctx->betaCachedRuns = 0;
+    }
+    auto ins = ctx->betaCache.emplace(key, tb);
+    if (ins.second) ctx->betaCachedRuns += static_cast<int64_t>(tb->end.size());
+    out = ins.first->second;
+    return RFMF_OK;
+}
+
+}  // namespace
+
+int build_beta_cached(rfmf_context* ctx, const double* t0s, int64_t C, int64_t total, BetaTables& bt) {
+    if (int rc = beta_range_check(t0s, C, total)) return rc;
+    bt = BetaTables{};
+    bt.chainOff.resize(C);
+    bt.chainRuns.resize(C);
+    std::map<uint64_t, std::pair<int64_t, int64_t>> placed;   // t0 bits -> (first run, runs)
+    for (int64_t c = 0; c < C; ++c) {
+        uint64_t bits;
+        std::memcpy(&bits, &t0s[c], sizeof bits);
+        auto it = placed.find(bits);
+        if (it == placed.end()) {
+            std::shared_ptr<const BetaRun> tb;
+            if (int rc = cached_runs(ctx, t0s[c], total, tb)) return rc;
+            const int64_t first = static_cast<int64_t>(bt.end.size());
+            if (first + static_cast<int64_t>(tb->end.size()) > kMaxBetaRuns)
+                return fail(RFMF_ERR_BETA_RUNS,
+                            "beta run tables exceed %lld runs (t0=%g, %lld sweeps); runs scale "
+                            "with log(sweeps)/t0 * 2^20",
+                            static_cast<long long>(kMaxBetaRuns), t0s[c], static_cast<long long>(total));
+            bt.end.insert(bt.end.end(), tb->end.begin(), tb->end.end());
+            bt.val.insert(bt.val.end(), tb->val.begin(), tb->val.end());
+            it = placed.emplace(bits, std::make_pair(first, static_cast<int64_t>(tb->end.size()))).first;
+        }
+        bt.chainOff[c] = it->second.first;
+        bt.chainRuns[c] = it->second.second;
     }
     return RFMF_OK;
 }

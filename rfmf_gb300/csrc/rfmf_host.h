@@ -7,7 +7,11 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/rfmf.h"
@@ -48,6 +52,12 @@ void gumbel_lut(int32_t lut[16]);
 
 // Run-length beta tables of a set of chains: one table per distinct t0,
 // chain c reads runs [chainOff[c], chainOff[c] + chainRuns[c]).
+// One t0's beta run table over a schedule's sweeps.
+struct BetaRun {
+    std::vector<int64_t> end;
+    std::vector<int32_t> val;
+};
+
 struct BetaTables {
     std::vector<int64_t> end;
     std::vector<int32_t> val;
@@ -55,6 +65,15 @@ struct BetaTables {
     std::vector<int64_t> chainRuns;
 };
 int build_beta(const double* t0s, int64_t C, int64_t total, BetaTables& bt);
+// One t0's run table over `total` sweeps, appended to end/val (the runs of
+// src/host_common.cpp:238-294); fails past kMaxBetaRuns entries in end.
+int append_runs(double t0, int64_t total, std::vector<int64_t>& end, std::vector<int32_t>& val);
+// Refuses t0s whose beta_fixed would overflow int32 within `total` sweeps.
+int beta_range_check(const double* t0s, int64_t C, int64_t total);
+constexpr int64_t kBetaCacheRuns = int64_t(1) << 24;
+// build_beta with each distinct t0's table taken from (or added to) the
+// context's cache; thread-safe.
+int build_beta_cached(rfmf_context* ctx, const double* t0s, int64_t C, int64_t total, BetaTables& bt);
 bool score_safe_int32(int64_t total, double t0, int64_t B);
 
 // Launch-shape helpers of the planner.
@@ -105,6 +124,13 @@ struct rfmf_context {
     int sms = 0;
     int smemOptin = 0;
     int32_t lut[16];
+    // Beta run tables per (t0 bits, sweeps), kept across batches and
+    // requests: most share their t0 ladder and length, and the tables are
+    // large (10^5 sweeps already hold ~30k runs per t0).  Dropped wholesale
+    // past kBetaCacheRuns runs.
+    std::mutex betaMu;
+    std::map<std::pair<uint64_t, uint64_t>, std::shared_ptr<const rfmf::BetaRun>> betaCache;
+    int64_t betaCachedRuns = 0;
 };
 
 // A graph in device memory: offsets and 8-byte entries for HBM walks, plus

@@ -47,6 +47,7 @@ struct Request {
     uint64_t total = 0;
     int pmax = 1;
     std::vector<uint32_t> initBits;   // C * words
+    BetaTables bt;                    // host run tables until admission
     // launch class
     int dbytes = 1, fmt = kCsrGlobal, W = 1;
     bool s64 = false;
@@ -131,6 +132,7 @@ struct rfmf_server {
     int64_t runningChains = 0;
     rfmf_server_stats stats{};
 
+
     // worker-owned
     std::thread worker;
     cudaStream_t stream = nullptr;
@@ -206,8 +208,7 @@ int admit(rfmf_server* s, Request& r) {
     const int64_t CW = r.C * r.words;
     int rc;
     if ((rc = r.dBits.alloc(CW * 4)) || (rc = r.dBest.alloc(CW * 4))) return rc;
-    BetaTables bt;
-    if ((rc = build_beta(r.t0s.data(), r.C, static_cast<int64_t>(r.total), bt))) return rc;
+    const BetaTables& bt = r.bt;
     if ((rc = r.dBetaEnd.alloc(bt.end.size() * 8)) || (rc = r.dBetaVal.alloc(bt.val.size() * 4)))
         return rc;
     const size_t np = std::max<size_t>(r.phaseP.size(), 1);
@@ -295,6 +296,7 @@ int admit(rfmf_server* s, Request& r) {
     CU(cudaStreamSynchronize(st));
     r.initBits.clear();
     r.initBits.shrink_to_fit();
+    r.bt = BetaTables{};
     return RFMF_OK;
 }
 
@@ -676,6 +678,11 @@ static int rfmf_submit_impl(rfmf_server* s, const rfmf_graph* g, int64_t nchains
         if (!(t0s[c] > 0.0)) return fail(RFMF_ERR_INVALID, "t0s[%lld] must be > 0", static_cast<long long>(c));
     r->total = total;
     r->pmax = static_cast<int>(std::max<uint64_t>(1, std::min<uint64_t>(maxP, static_cast<uint64_t>(g->n))));
+    // Run tables on the submitting thread (from the context's cache when
+    // another batch or request used the same t0 and length), never on the
+    // worker, where building them would stall the launch windows.
+    if (int rc = build_beta_cached(s->ctx, r->t0s.data(), nchains, static_cast<int64_t>(total), r->bt))
+        return rc;
 
     // launch class
     const rfmf_launch_config& c = s->lc;

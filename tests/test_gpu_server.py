@@ -116,3 +116,25 @@ def test_server_errors(rfmf, ctx):
     assert st["state"] == "done"
     srv.result(rid)
     srv.close()
+
+
+def test_shared_beta_tables_and_refusal_at_submit(rfmf, ctx):
+    """Requests sharing a t0 ladder and length reuse one set of run tables
+    (built on the submitting thread) and still equal standalone anneals; a
+    schedule whose beta would overflow int32 is refused by rfmf_submit itself,
+    before any device state, as rfmf_anneal refuses it."""
+    g = rfmf.erdos_renyi(400, 0.04, signed=True, seed=8)
+    dg = rfmf.DeviceGraph(ctx, g)
+    ladder = [35.0, 50.0, 70.0, 100.0]
+    reqs = [_request(rfmf, g, list(range(500 + 20 * k, 512 + 20 * k)), ladder * 3, [32, 4, 1],
+                     [400, 400, 400]) for k in range(3)]
+    srv = rfmf.Server(ctx, window_sweeps=300)
+    ids = [srv.submit(dg, r["init"], r["t0s"], r["phases"], r["iters"], r["solver"]) for r in reqs]
+    for rid, r in zip(ids, reqs):
+        st = srv.wait(rid, timeout=300)
+        assert st["state"] == "done", st
+        _same(srv.result(rid), _standalone(rfmf, ctx, dg, r))
+    bad = _request(rfmf, g, [1, 2], [1e-9, 35.0], [8, 1], [10**6, 10**6])
+    with pytest.raises(rfmf.RfmfError):
+        srv.submit(dg, bad["init"], bad["t0s"], bad["phases"], bad["iters"], bad["solver"])
+    srv.close()
