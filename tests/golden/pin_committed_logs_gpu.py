@@ -106,11 +106,16 @@ def main():
     record["gpu_entries"] = [x for x in record.get("gpu_entries", [])
                              if (x["results"], x["graph"], x["chain"]) not in keys] + entries
     import torch
-    record["gpu_run"] = dict(device=torch.cuda.get_device_name(0), sm_count=ctx.info()["sm_count"],
-                             chains=len(entries), sweeps_per_chain=total,
-                             seconds=round(el, 1), window=a.window,
-                             ingest="native parser + CSR built on the GPU" if a.device_ingest
-                             else "Python reader + host CSR")
+    runs = record.get("gpu_runs", {})
+    if "gpu_run" in record:     # single-run records kept before per-set runs
+        runs.setdefault("V100-SXM2-10M", record.pop("gpu_run"))
+    for rs in sorted({c["results"] for c in spec}):
+        runs[rs] = dict(device=torch.cuda.get_device_name(0), sm_count=ctx.info()["sm_count"],
+                        chains=len(entries), sweeps_per_chain=total,
+                        seconds=round(el, 1), window=a.window,
+                        ingest="native parser + CSR built on the GPU" if a.device_ingest
+                        else "Python reader + host CSR")
+    record["gpu_runs"] = runs
     OUT.write_text(json.dumps(record, indent=1) + "\n")
     return 0 if nmatch == len(entries) else 1
 
