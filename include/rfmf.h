@@ -242,7 +242,7 @@ typedef struct rfmf_batch_plan {
     int csr_format;            /* 1 unit16, 2 packed32, 3 HBM */
     int gain_width;            /* bytes per vertex gain: 1 or 4 */
     int smem_bytes;            /* dynamic shared memory per CTA */
-    int balanced;              /* 1 once work items are sized from learned graph costs */
+    int balanced;              /* 1 once every multi-graph launch class sizes its work items from learned graph costs */
     int launch_classes;        /* launches per window (graphs grouped by kernel variant and size) */
 } rfmf_batch_plan;
 

@@ -784,7 +784,7 @@ extern "C" int rfmf_batch_info(const rfmf_batch* b, rfmf_batch_plan* out) {
         if (k.order.size() > most) { most = k.order.size(); big = &k; }
         grid += k.grid;
         items += k.nitems;
-        balanced = balanced && k.balanced;
+        balanced = balanced && (k.balanced || k.graphs.size() < 2);   // one graph: nothing to balance
     }
     out->nchains = b->C;
     out->total_sweeps = b->total;
