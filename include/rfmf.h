@@ -225,6 +225,12 @@ int rfmf_batch_stats(rfmf_batch* b, uint64_t* improved_sweeps);
 /* Wait for the batch's work; reports a device-side error if one occurred. */
 int rfmf_batch_synchronize(rfmf_batch* b);
 
+/* Testing aid for the failure path: overwrite chain `chain`'s carried cut
+ * value on the device (after the batch's queued work).  The next launch
+ * finds it inconsistent with the chain's spins and the batch reports
+ * RFMF_ERR_DEVICE; the context stays usable.  No GPU fault is involved. */
+int rfmf_batch_debug_set_cut(rfmf_batch* b, int64_t chain, int64_t cut);
+
 /* Copy chain state to the host (synchronous).  Any pointer may be NULL.
  * end_spins/best_spins: concatenated like initial_spins. */
 int rfmf_batch_read(rfmf_batch* b, int8_t* end_spins, int8_t* best_spins,

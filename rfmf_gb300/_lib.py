@@ -40,6 +40,7 @@ SIGNATURES = [
     ("rfmf_batch_run_graph", ct.c_int, [_P, _U64, ct.c_int, ct.c_int]),
     ("rfmf_batch_run_timed", ct.c_int, [_P, _U64, _P]),
     ("rfmf_batch_stats", ct.c_int, [_P, _P]),
+    ("rfmf_batch_debug_set_cut", ct.c_int, [_P, _I64, _I64]),
     ("rfmf_batch_synchronize", ct.c_int, [_P]),
     ("rfmf_batch_read", ct.c_int, [_P, _P, _P, _P, _P, _P]),
     ("rfmf_batch_info", ct.c_int, [_P, _P]),

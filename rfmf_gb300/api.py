@@ -283,6 +283,10 @@ class Batch:
         check(lib().rfmf_batch_stats(self.h, _p(out)))
         return out
 
+    def debug_set_cut(self, chain, cut):
+        """Testing aid: overwrite a chain's carried cut on the device."""
+        check(lib().rfmf_batch_debug_set_cut(self.h, int(chain), int(cut)))
+
     def synchronize(self):
         check(lib().rfmf_batch_synchronize(self.h))
 

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -935,6 +936,15 @@ extern "C" int rfmf_batch_stats(rfmf_batch* b, uint64_t* improved_sweeps) {
     } catch (...) {
         return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_batch_stats");
     }
+}
+
+extern "C" int rfmf_batch_debug_set_cut(rfmf_batch* b, int64_t chain, int64_t cut) {
+    if (!b || chain < 0 || chain >= b->C) return rfmf::fail(RFMF_ERR_INVALID, "batch is NULL or chain out of range");
+    CU(cudaSetDevice(b->ctx->device));
+    CU(cudaStreamSynchronize(b->ctx->stream));
+    char* rec = static_cast<char*>(b->dChains.p) + chain * static_cast<int64_t>(sizeof(DevChain));
+    CU(cudaMemcpy(rec + offsetof(DevChain, cur), &cut, sizeof cut, cudaMemcpyHostToDevice));
+    return RFMF_OK;
 }
 
 extern "C" int rfmf_batch_synchronize(rfmf_batch* b) {
