@@ -376,45 +376,82 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
         const int dbytes = c.gain_width ? c.gain_width : (g->B <= 127 ? 1 : 4);
         if (dbytes == 1 && g->B > 127)
             return fail(RFMF_ERR_INVALID, "int8 gains need max weighted degree <= 127 (B=%lld)", (long long)g->B);
-        const int W = choose_warps(static_cast<int>(g->n), c, b->C, ctx->sms);
-        bool s64 = (c.score_path == 2);
-        if (!s64) {
-            for (int32_t ch : chainsOfGraph[gi])
-                if (!compact_key_safe(static_cast<int64_t>(total), t0s[ch], g->B, key_bits(g->n, 32 * W))) {
-                    s64 = true;
-                    break;
-                }
-            if (s64 && c.score_path == 1)
-                return fail(RFMF_ERR_INVALID, "int32 scores would overflow for this (t0, B, sweeps)");
-        }
         const int pmaxG = static_cast<int>(std::max<uint64_t>(1, std::min<uint64_t>(maxP, static_cast<uint64_t>(g->n))));
-        const uint32_t chainB = chain_layout(static_cast<int>(g->n), static_cast<int>((g->n + 31) / 32), pmaxG, W,
-                                             dbytes).total;
-        int fmt = kCsrGlobal;
-        // A shared-memory CSR pays only while it leaves room for the chains a
-        // CTA should hold: about 8 warps, fewer when the graph has fewer
-        // chains or the batch fewer than that per SM.  Otherwise its rows are
-        // walked in HBM (L2-resident) and the CTA holds more chains.
         const int64_t perSm = (b->C + ctx->sms - 1) / std::max(ctx->sms, 1);
-        const int64_t kWant = std::max<int64_t>(
-            1, std::min<int64_t>({static_cast<int64_t>(chainsOfGraph[gi].size()),
-                                  static_cast<int64_t>(std::max(1, 8 / W)), perSm}));
-        auto fits = [&](int f) {
-            cudaFuncAttributes fa{};
-            const int64_t dynMax = dyn_smem_max(ctx, kernel_ptr(dbytes, f, s64), fa);
-            return dynMax > 0 &&
-                   static_cast<int64_t>(kSmemHeader) + csr_bytes(g, f) + kWant * chainB <= dynMax;
+        // Kernel variant, CSR format and chains resident per SM of this graph
+        // at Wc warps per chain.
+        struct Pick {
+            bool s64 = false;
+            int fmt = kCsrGlobal;
+            int64_t resident = 0;
         };
-        if (c.csr_format == 1) {
-            if (!g->unit16) return fail(RFMF_ERR_INVALID, "unit16 CSR needs |w| == 1 and n <= 32768");
-            fmt = kCsrUnit16;
-        } else if (c.csr_format == 2) {
-            if (!g->packed32) return fail(RFMF_ERR_INVALID, "packed32 CSR needs |w| < 2^15 and n <= 65536");
-            fmt = kCsrPacked32;
-        } else if (c.csr_format == 0) {
-            if (g->unit16 && fits(kCsrUnit16)) fmt = kCsrUnit16;
-            else if (g->packed32 && fits(kCsrPacked32)) fmt = kCsrPacked32;
+        auto pick = [&](int Wc, Pick& pk) -> int {
+            pk = Pick{};
+            pk.s64 = (c.score_path == 2);
+            if (!pk.s64) {
+                for (int32_t ch : chainsOfGraph[gi])
+                    if (!compact_key_safe(static_cast<int64_t>(total), t0s[ch], g->B, key_bits(g->n, 32 * Wc))) {
+                        pk.s64 = true;
+                        break;
+                    }
+                if (pk.s64 && c.score_path == 1)
+                    return fail(RFMF_ERR_INVALID, "int32 scores would overflow for this (t0, B, sweeps)");
+            }
+            const int64_t chainB = chain_layout(static_cast<int>(g->n), static_cast<int>((g->n + 31) / 32), pmaxG,
+                                                Wc, dbytes).total;
+            // A shared-memory CSR pays only while it leaves room for the chains
+            // a CTA should hold: about 8 warps, fewer when the graph has fewer
+            // chains or the batch fewer than that per SM.  Otherwise its rows
+            // are walked in HBM (L2-resident) and the CTA holds more chains.
+            const int64_t kWant = std::max<int64_t>(
+                1, std::min<int64_t>({static_cast<int64_t>(chainsOfGraph[gi].size()),
+                                      static_cast<int64_t>(std::max(1, 8 / Wc)), perSm}));
+            auto fits = [&](int f) {
+                cudaFuncAttributes fa{};
+                const int64_t dynMax = dyn_smem_max(ctx, kernel_ptr(dbytes, f, pk.s64), fa);
+                return dynMax > 0 &&
+                       static_cast<int64_t>(kSmemHeader) + csr_bytes(g, f) + kWant * chainB <= dynMax;
+            };
+            if (c.csr_format == 1) {
+                if (!g->unit16) return fail(RFMF_ERR_INVALID, "unit16 CSR needs |w| == 1 and n <= 32768");
+                pk.fmt = kCsrUnit16;
+            } else if (c.csr_format == 2) {
+                if (!g->packed32) return fail(RFMF_ERR_INVALID, "packed32 CSR needs |w| < 2^15 and n <= 65536");
+                pk.fmt = kCsrPacked32;
+            } else if (c.csr_format == 0) {
+                if (g->unit16 && fits(kCsrUnit16)) pk.fmt = kCsrUnit16;
+                else if (g->packed32 && fits(kCsrPacked32)) pk.fmt = kCsrPacked32;
+            }
+            cudaFuncAttributes fa{};
+            const int64_t dynMax = dyn_smem_max(ctx, kernel_ptr(dbytes, pk.fmt, pk.s64), fa);
+            const int64_t room = dynMax - static_cast<int64_t>(kSmemHeader) -
+                                 (pk.fmt == kCsrGlobal ? 0 : static_cast<int64_t>(csr_bytes(g, pk.fmt)));
+            const int64_t warpCap = std::min(16 / Wc, Wc > 1 ? 15 : 16);
+            pk.resident = std::max<int64_t>(0, std::min<int64_t>({perSm, warpCap, room / chainB}));
+            return RFMF_OK;
+        };
+        int W = choose_warps(static_cast<int>(g->n), c, b->C, ctx->sms);
+        Pick pk;
+        if (int rc = pick(W, pk)) return rc;
+        // When shared memory (not the chain count) keeps an SM's chains from
+        // all being resident, wider chains fill the idle warp slots: widen
+        // while that raises the warps resident per SM (GB300, 2432 chains:
+        // ER n = 5000 d = 5 169 -> 216 M chain-steps/s at two warps, random
+        // tree n = 10000 106 -> 112 at four).  Only within about two waves of
+        // one-warp chains per SM: deeper queues keep every warp slot busy
+        // anyway and one warp per chain does more per slot (512 graphs x 64
+        // chains: 1.52e8 -> 1.44e8 when widened).
+        if (c.threads_per_chain == 0 && perSm <= 32) {
+            while (W < kMaxAutoWarps && pk.resident < perSm) {
+                Pick wider;
+                if (int rc = pick(2 * W, wider)) return rc;
+                if (2 * W * wider.resident <= W * pk.resident) break;
+                W *= 2;
+                pk = wider;
+            }
         }
+        const bool s64 = pk.s64;
+        const int fmt = pk.fmt;
         const Key key{dbytes, fmt, W, s64 ? 1 : 0};
         auto it = classOf.find(key);
         if (it == classOf.end()) {
