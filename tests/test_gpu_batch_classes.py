@@ -81,3 +81,21 @@ def test_auto_warps_follow_chain_count(rfmf, ctx):
         b.close()
     assert widths[32] > 32, widths
     assert widths[8 * sms] == 32, widths
+
+
+def test_widening_when_shared_memory_limits_residency(rfmf, ctx):
+    """16 chains per SM of ER n = 5000 (mean degree 5): with one warp each
+    only ~12 fit an SM's shared memory beside the graph, so the planner gives
+    each chain two warps (16 warps resident); the same graph with 8 chains
+    per SM keeps them all resident at one warp each."""
+    g = rfmf.erdos_renyi_sparse(5000, 5, signed=True, seed=0)
+    dg = rfmf.DeviceGraph(ctx, g)
+    sms = ctx.info()["sm_count"]
+    widths = {}
+    for C in (8 * sms, 16 * sms):
+        init, solver = chains_for(g, list(range(C)))
+        b = rfmf.Batch(ctx, [dg] * C, [70.0] * C, solver, list(init), [8, 1], [4, 4])
+        widths[C] = b.info()["threads_per_chain"]
+        b.close()
+    assert widths[16 * sms] == 64, widths
+    assert widths[8 * sms] == 32, widths
