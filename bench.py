@@ -67,9 +67,10 @@ def chain_setup(graphs, chains_per_graph, seed_base):
     return per
 
 
-def schedule(sweeps):
-    per = sweeps // len(PHASES)
-    return PHASES, [per] * len(PHASES)
+def schedule(sweeps, phases=None):
+    phases = list(phases or PHASES)
+    per = sweeps // len(phases)
+    return phases, [per] * len(phases)
 
 
 def sweep_bytes(n, m, P):
@@ -254,10 +255,12 @@ def gpu_arm(args, rank, world):
     dgs = [R.DeviceGraph(ctx, g) for g in graphs]
     K, W = args.steps, args.warmup
     sweeps = args.sweeps
-    if sweeps % (8 * K):
-        sweeps = (sweeps // (8 * K)) * 8 * K
+    main_phases = [int(x) for x in str(args.phases).split(",")] if args.phases else PHASES
+    q = len(main_phases) * K
+    if sweeps % q:
+        sweeps = (sweeps // q) * q
     per_step = sweeps // K
-    phases, iters = schedule(sweeps)
+    phases, iters = schedule(sweeps, main_phases)
     cfg = R.make_config(threads_per_chain=args.threads, chains_per_cta=args.chains_per_cta)
     base = rank * args.chains
     setup = chain_setup(graphs, args.chains, base)
@@ -379,7 +382,7 @@ def gpu_arm(args, rank, world):
             "chains_per_graph": args.chains,
             "sweeps_per_chain": sweeps,
             "sweeps_per_step": per_step,
-            "phases": PHASES,
+            "phases": phases,
             "t0_ladder": LADDER,
             "threads_per_chain": info["threads_per_chain"],
             "chains_per_cta": info["chains_per_cta"],
@@ -704,6 +707,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--sweeps", type=int, default=10_000_000)
+    ap.add_argument("--phases", default=None,
+                    help="comma list of P for the main workload (default 128,...,1; profiling cases "
+                         "use one phase)")
     ap.add_argument("--chains", type=int, default=1024)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--chains-per-cta", type=int, default=0)
