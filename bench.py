@@ -49,8 +49,19 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
-def workload_graphs():
+# The large sparse shapes (100x200 torus, random tree n = 10000, ER n = 5000
+# mean degree 5; 256 chains each): a profiling and parity workload whose
+# CSRs do not all fit shared memory beside the chains (the HBM walk).
+LARGE_WORKLOAD = "torus100x200_pm1+tree10000+er5000_d5_pm1"
+WORKLOAD_CHAINS = {WORKLOAD: 1024, LARGE_WORKLOAD: 256}
+
+
+def workload_graphs(name=WORKLOAD):
     import rfmf_gb300 as R
+    if name == LARGE_WORKLOAD:
+        return [R.torus(100, 200, signed=True, seed=0, name="torus100x200"),
+                R.random_tree(10000, seed=0, name="tree10000"),
+                R.erdos_renyi_sparse(5000, 5, signed=True, seed=0, name="er5000_d5")]
     return [R.torus(50, 60, signed=True, seed=0, name="torus50x60"),
             R.erdos_renyi_degree(2000, 19, signed=True, seed=0, name="er2000_d19")]
 
@@ -251,7 +262,7 @@ def gpu_arm(args, rank, world):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     ctx = R.Context(dev)
-    graphs = workload_graphs()
+    graphs = workload_graphs(args.workload)
     dgs = [R.DeviceGraph(ctx, g) for g in graphs]
     K, W = args.steps, args.warmup
     sweeps = args.sweeps
@@ -375,9 +386,11 @@ def gpu_arm(args, rank, world):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "int32",
-        "data": "synthetic (seeded torus 50x60 +-1 and Erdos-Renyi n=2000 d~19 +-1)",
+        "data": ("synthetic (seeded torus 50x60 +-1 and Erdos-Renyi n=2000 d~19 +-1)"
+                 if args.workload == WORKLOAD else
+                 "synthetic (seeded torus 100x200 +-1, random tree n=10000 +1, Erdos-Renyi n=5000 d~5 +-1)"),
         "config": {
-            "workload": WORKLOAD,
+            "workload": args.workload,
             "graphs": [dict(name=g.name, n=g.n, m=g.m, B=g.max_weighted_degree()) for g in graphs],
             "chains_per_graph": args.chains,
             "sweeps_per_chain": sweeps,
@@ -710,7 +723,10 @@ def main():
     ap.add_argument("--phases", default=None,
                     help="comma list of P for the main workload (default 128,...,1; profiling cases "
                          "use one phase)")
-    ap.add_argument("--chains", type=int, default=1024)
+    ap.add_argument("--chains", type=int, default=None, help="chains per graph (default per workload)")
+    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, LARGE_WORKLOAD],
+                    help="the headline mid-size workload (default) or the large sparse shapes, "
+                         "a profiling case (no e2e, CPU or plain-kernel legs)")
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--chains-per-cta", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
@@ -727,6 +743,10 @@ def main():
     ap.add_argument("--serve-sweeps", type=int, default=100_000)
     ap.add_argument("--serve-window", type=int, default=4096)
     args = ap.parse_args()
+    if args.chains is None:
+        args.chains = WORKLOAD_CHAINS[args.workload]
+    if args.workload != WORKLOAD:
+        args.no_e2e = args.no_cpu = args.no_plain = True
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
