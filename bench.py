@@ -373,7 +373,9 @@ def gpu_arm(args, rank, world):
     sm_mhz = clk["sm_mhz"] or peaks.get("sm_max_mhz", 2070.0)
     smem_peak = sm_count * 128.0 * sm_mhz * 1e6 / 1e9   # GB/s
     achieved = sum(step_bytes) / (total_ms / 1e3) / 1e9
-    traffic = profile_traffic()
+    # The committed profile figures (DRAM bytes and instructions per
+    # chain-sweep) describe the headline workload's kernel only.
+    traffic = profile_traffic() if args.workload == WORKLOAD else None
     result = {
         "metric": "chain-steps/s",
         "value": value,
