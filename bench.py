@@ -613,10 +613,14 @@ def serving_graphs():
 
 def serving_arm(args, ctx, rate):
     """Continuous batching through the request server: Poisson arrivals at
-    `rate` req/s for `seconds`; each request draws a graph from the
-    large-sparse families (torus, tree, ER d=5; n 5000-20000), 16-256 chains
-    and a budget of args.serve_sweeps sweeps (default schedule).  Latency =
-    submit -> results on the host (server clock)."""
+    `rate` req/s for `seconds`, or until args.serve_max_requests have
+    arrived (which bounds the high-rate runs: at 2000 req/s the cap's
+    requests arrive in a fraction of a second and the run measures the
+    saturated server); each request draws a graph from the large-sparse
+    families (torus, tree, ER d=5; n 5000-20000), 16-256 chains and a budget
+    of args.serve_sweeps sweeps (default schedule).  Latency = submit ->
+    results on the host (server clock).  `offered_rate_req_s` is the rate at
+    which the submitting thread actually handed requests to the server."""
     import threading
 
     import rfmf_gb300 as R
@@ -626,11 +630,12 @@ def serving_arm(args, ctx, rate):
     seconds = args.serve_seconds
     arrivals = []
     t = 0.0
-    while True:
+    while len(arrivals) < args.serve_max_requests:
         t += float(rng.exponential(1.0 / rate))
         if t > seconds:
             break
         arrivals.append(t)
+    submitted = [0.0] * len(arrivals)
     reqs = [dict(g=int(rng.integers(len(graphs))), C=int(rng.choice([16, 32, 64, 128, 256])),
                  seed0=10_000_000 + 1000 * i) for i in range(len(arrivals))]
     phases, iters = schedule(args.serve_sweeps)
@@ -638,18 +643,27 @@ def serving_arm(args, ctx, rate):
     ids = [None] * len(reqs)
     err = []
 
+    # Request inputs are built before the arrival stream starts, so that the
+    # submitting thread only calls submit (building initial spins in the loop
+    # had capped the offered rate near 180 req/s).
+    inputs = []
+    for r in reqs:
+        g = graphs[r["g"]]
+        seeds = [r["seed0"] + k for k in range(r["C"])]
+        inputs.append((np.stack([R.initial_spins(x, g.n) for x in seeds]),
+                       [LADDER[k % 8] for k in range(r["C"])],
+                       [R.solver_seed(x) for x in seeds]))
+
     def submitter():
         t0 = time.perf_counter()
         for i, (at, r) in enumerate(zip(arrivals, reqs)):
-            g = graphs[r["g"]]
-            seeds = [r["seed0"] + k for k in range(r["C"])]
-            init = np.stack([R.initial_spins(x, g.n) for x in seeds])
+            init, t0s, solver = inputs[i]
             d = at - (time.perf_counter() - t0)
             if d > 0:
                 time.sleep(d)
             try:
-                ids[i] = srv.submit(dgs[r["g"]], init, [LADDER[k % 8] for k in range(r["C"])],
-                                    phases, iters, [R.solver_seed(x) for x in seeds])
+                ids[i] = srv.submit(dgs[r["g"]], init, t0s, phases, iters, solver)
+                submitted[i] = time.perf_counter() - t0
             except Exception as e:   # pragma: no cover
                 err.append(repr(e))
                 return
@@ -675,7 +689,10 @@ def serving_arm(args, ctx, rate):
     stats = srv.stats()
     srv.close()
     lat = np.array(lat)
-    return {"rate_req_s": rate, "requests": len(reqs), "duration_s": seconds,
+    span = submitted[-1] - submitted[0] if len(submitted) > 1 else 0.0
+    return {"rate_req_s": rate, "requests": len(reqs),
+            "arrival_window_s": arrivals[-1] if arrivals else 0.0,
+            "offered_rate_req_s": (len(submitted) - 1) / span if span > 0 else None,
             "sweeps_per_request": args.serve_sweeps, "window_sweeps": args.serve_window,
             "latency_p50_s": float(np.percentile(lat, 50)),
             "latency_p99_s": float(np.percentile(lat, 99)),
@@ -740,8 +757,12 @@ def main():
     ap.add_argument("--batched-graphs", type=int, default=512)
     ap.add_argument("--batched-sweeps", type=int, default=2000)
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--serve-rate", default="2,10", help="req/s; a comma list sweeps several rates")
-    ap.add_argument("--serve-seconds", type=float, default=20.0)
+    ap.add_argument("--serve-rate", default="2,10,100,2000",
+                    help="req/s; a comma list sweeps several rates")
+    ap.add_argument("--serve-seconds", type=float, default=20.0,
+                    help="longest arrival window per rate")
+    ap.add_argument("--serve-max-requests", type=int, default=200,
+                    help="arrivals per rate at most (bounds the high-rate runs)")
     ap.add_argument("--serve-sweeps", type=int, default=100_000)
     ap.add_argument("--serve-window", type=int, default=4096)
     args = ap.parse_args()

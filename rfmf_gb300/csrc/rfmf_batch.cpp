@@ -582,9 +582,8 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
     {
         size_t sp = 0;
         for (int64_t i = 0; i < C; ++i) {
-            uint32_t* w = bits.data() + b->chainWordOff[i];
-            for (int64_t v = 0; v < b->chainN[i]; ++v, ++sp)
-                if (initial_spins[sp] >= 0) w[v >> 5] |= 1u << (v & 31);
+            pack_spins(initial_spins + sp, b->chainN[i], bits.data() + b->chainWordOff[i]);
+            sp += static_cast<size_t>(b->chainN[i]);
         }
     }
 
@@ -760,9 +759,8 @@ static int rfmf_batch_read_impl(rfmf_batch* b, int8_t* end_spins, int8_t* best_s
         CU(cudaMemcpy(w.data(), src.p, w.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
         size_t sp = 0;
         for (int64_t i = 0; i < b->C; ++i) {
-            const uint32_t* cw = w.data() + b->chainWordOff[i];
-            for (int64_t v = 0; v < b->chainN[i]; ++v, ++sp)
-                dst[sp] = ((cw[v >> 5] >> (v & 31)) & 1u) ? 1 : -1;
+            unpack_spins(w.data() + b->chainWordOff[i], b->chainN[i], dst + sp);
+            sp += static_cast<size_t>(b->chainN[i]);
         }
         return RFMF_OK;
     };

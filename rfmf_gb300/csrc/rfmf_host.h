@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -115,6 +116,59 @@ struct DevBuf {
     }
     template <class T> T* as() const { return static_cast<T*>(p); }
 };
+
+// One chain's spins (int8, >= 0 is +1) as ceil(n/32) words, bit v = spin +1;
+// every word is written (tail bits past n are 0).  Eight spins at a time:
+// byte k of m is 1 where spin k >= 0 (its sign bit clear), and multiplying
+// by sum_k 2^(56-7k) moves byte k's bit to bit 56+k with no two partial
+// products overlapping, so the top byte is the eight bits in order.
+static_assert(__BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__, "spin packing assumes little-endian bytes");
+inline uint32_t pack_spin_bytes8(const int8_t* s) {
+    uint64_t u;
+    std::memcpy(&u, s, 8);
+    const uint64_t m = (~u >> 7) & 0x0101010101010101ull;
+    return static_cast<uint32_t>((m * 0x0102040810204080ull) >> 56);
+}
+
+inline void pack_spins(const int8_t* sp, int64_t n, uint32_t* words) {
+    const int64_t full = n >> 5;
+    for (int64_t w = 0; w < full; ++w) {
+        const int8_t* s = sp + 32 * w;
+        words[w] = pack_spin_bytes8(s) | (pack_spin_bytes8(s + 8) << 8) |
+                   (pack_spin_bytes8(s + 16) << 16) | (pack_spin_bytes8(s + 24) << 24);
+    }
+    if (n & 31) {
+        const int8_t* s = sp + 32 * full;
+        uint32_t x = 0;
+        for (int j = 0; j < static_cast<int>(n & 31); ++j) x |= static_cast<uint32_t>(s[j] >= 0) << j;
+        words[full] = x;
+    }
+}
+
+// The inverse: spins[v] = +1 where bit v is set, else -1.  Eight at a time:
+// the byte replicated eight times and masked with bit k in byte k leaves
+// byte k nonzero iff bit k is set; adding 0x7F per byte (no carries: every
+// byte is 0 or a single bit <= 0x80) sets its top bit iff nonzero; c * 0xFE
+// xor 0xFF per byte is 0x01 (+1) for c = 1 and 0xFF (-1) for c = 0.
+inline void unpack_spins(const uint32_t* words, int64_t n, int8_t* sp) {
+    const int64_t full = n >> 5;
+    for (int64_t w = 0; w < full; ++w) {
+        const uint32_t x = words[w];
+        for (int q = 0; q < 4; ++q) {
+            const uint64_t t = (static_cast<uint64_t>((x >> (8 * q)) & 0xFFu) * 0x0101010101010101ull) &
+                               0x8040201008040201ull;
+            const uint64_t c = ((t + 0x7F7F7F7F7F7F7F7Full) >> 7) & 0x0101010101010101ull;
+            const uint64_t out = ~0ull ^ (c * 0xFEull);
+            std::memcpy(sp + 32 * w + 8 * q, &out, 8);
+        }
+    }
+    if (n & 31) {
+        const uint32_t x = words[full];
+        int8_t* s = sp + 32 * full;
+        for (int j = 0; j < static_cast<int>(n & 31); ++j)
+            s[j] = static_cast<int8_t>(2 * static_cast<int>((x >> j) & 1u) - 1);
+    }
+}
 
 }  // namespace rfmf
 

@@ -731,12 +731,8 @@ static int rfmf_submit_impl(rfmf_server* s, const rfmf_graph* g, int64_t nchains
     r->fmt = fmt;
     if (nchains * r->words > (int64_t(1) << 34)) return fail(RFMF_ERR_CAPACITY, "request too large");
     r->initBits.assign(static_cast<size_t>(nchains * r->words), 0u);
-    for (int64_t k = 0; k < nchains; ++k) {
-        uint32_t* w = r->initBits.data() + k * r->words;
-        const int8_t* sp = initial_spins + k * g->n;
-        for (int64_t v = 0; v < g->n; ++v)
-            if (sp[v] >= 0) w[v >> 5] |= 1u << (v & 31);
-    }
+    for (int64_t k = 0; k < nchains; ++k)
+        pack_spins(initial_spins + k * g->n, g->n, r->initBits.data() + k * r->words);
     {
         std::lock_guard<std::mutex> lk(s->mu);
         r->id = s->nextId++;
@@ -795,12 +791,8 @@ static int rfmf_result_impl(rfmf_server* s, uint64_t request_id, int8_t* end_spi
         s->all.erase(it);
     }
     for (int64_t c = 0; c < r->C; ++c) {
-        const uint32_t* e = r->endBits.data() + c * r->words;
-        const uint32_t* b = r->bestBits.data() + c * r->words;
-        for (int64_t v = 0; v < r->n; ++v) {
-            if (end_spins) end_spins[c * r->n + v] = ((e[v >> 5] >> (v & 31)) & 1u) ? 1 : -1;
-            if (best_spins) best_spins[c * r->n + v] = ((b[v >> 5] >> (v & 31)) & 1u) ? 1 : -1;
-        }
+        if (end_spins) unpack_spins(r->endBits.data() + c * r->words, r->n, end_spins + c * r->n);
+        if (best_spins) unpack_spins(r->bestBits.data() + c * r->words, r->n, best_spins + c * r->n);
         if (best_vals) best_vals[c] = r->best[c];
         if (final_vals) final_vals[c] = r->cur[c];
     }

@@ -285,3 +285,31 @@ def test_matches_reference_kernel_fixtures(rfmf, ctx, case):
     assert [int(x) for x in res.final_vals] == case["final"]
     assert [M.psha(x) for x in res.best_spins] == case["best_partition_sha256"]
     assert [M.psha(x) for x in res.end_spins] == case["final_partition_sha256"]
+
+
+def test_best_cut_distribution_64_seeds(rfmf, ctx):
+    """The distributional fallback of the parity bar: over 64 seeds, the
+    best-cut distribution of librfmf.so against the reference kernel's run of
+    the same 64 chains (50x60 torus, +-1 weights, phases 128..1, t0 ladder)
+    must pass a two-sample KS test at p > 0.05.  The path is bit-exact, so
+    the statistic is 0 here; the chain-for-chain equality is asserted too."""
+    import json
+    import sys
+
+    from conftest import GOLDEN, ROOT
+    stats = pytest.importorskip("scipy.stats")
+    sys.path.insert(0, str(ROOT / "tests" / "golden"))
+    import make_refkernel_golden as M
+
+    case = next(c for c in json.loads((GOLDEN / "refkernel_runs.json").read_text())["cases"]
+                if c["name"] == "torus50x60_pm1")
+    assert len(case["seeds"]) == 64
+    g = M.build_graph(tuple(case["graph"]))
+    init, solver = chains_for(g, case["seeds"])
+    dg = rfmf.DeviceGraph(ctx, g)
+    res = rfmf.anneal_gpu(ctx, dg, g.max_weighted_degree(), init, case["t0s"], case["phases"],
+                          case["iters"], solver)
+    ours = [int(x) for x in res.best_vals]
+    ks = stats.ks_2samp(ours, case["best"])
+    assert ks.pvalue > 0.05
+    assert ks.statistic == 0.0 and ours == case["best"]
