@@ -284,6 +284,9 @@ typedef struct rfmf_server_config {
     uint64_t window_sweeps;      /* sweeps per launch window (0 = 4096) */
     int64_t max_chains;          /* chains admitted at once (0 = 1 << 20); later requests queue */
     rfmf_launch_config launch;   /* threads_per_chain / gain_width / csr_format / score_path */
+    int64_t max_device_bytes;    /* device bytes of the admitted requests' own state at once
+                                    (0 = no limit); later requests queue, and a request that
+                                    alone exceeds it is refused (RFMF_ERR_CAPACITY) */
 } rfmf_server_config;
 
 enum rfmf_request_state {

@@ -85,7 +85,7 @@ class BatchPlan(ct.Structure):
 class ServerConfig(ct.Structure):
     """rfmf_server_config."""
     _fields_ = [("window_sweeps", ct.c_uint64), ("max_chains", ct.c_int64),
-                ("launch", LaunchConfig)]
+                ("launch", LaunchConfig), ("max_device_bytes", ct.c_int64)]
 
 
 class RequestStatus(ct.Structure):

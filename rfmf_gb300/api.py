@@ -340,11 +340,12 @@ class Server:
     then take the results.  Each request's results equal anneal_gpu on the
     same inputs."""
 
-    def __init__(self, ctx, window_sweeps=4096, max_chains=0, cfg=None):
+    def __init__(self, ctx, window_sweeps=4096, max_chains=0, cfg=None, max_device_bytes=0):
         sc = ServerConfig()
         sc.window_sweeps = int(window_sweeps)
         sc.max_chains = int(max_chains)
         sc.launch = cfg or make_config()
+        sc.max_device_bytes = int(max_device_bytes)
         h = ct.c_void_p()
         check(lib().rfmf_server_create(ctx.h, ct.byref(sc), ct.byref(h)))
         self.h = h

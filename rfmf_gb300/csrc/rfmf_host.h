@@ -117,6 +117,26 @@ struct DevBuf {
     template <class T> T* as() const { return static_cast<T*>(p); }
 };
 
+// Request server admission.  A request's own device state: its spin and
+// best-spin words, beta run tables (8 + 4 bytes a run), schedule (4 + 8 bytes
+// a phase) and chain records; a DevBuf holds at least 16 bytes.
+inline int64_t request_device_bytes(int64_t C, int64_t words, int64_t betaRuns, int64_t nphases) {
+    auto buf = [](int64_t b) { return b < 16 ? int64_t(16) : b; };
+    const int64_t np = nphases > 1 ? nphases : 1;
+    return 2 * buf(C * words * 4) + buf(betaRuns * 8) + buf(betaRuns * 4) + buf(np * 4) +
+           buf(np * 8) + C * static_cast<int64_t>(sizeof(DevChain));
+}
+
+// The queue head joins the running requests while the admitted chains and
+// device bytes stay within max_chains and max_device_bytes (0: no byte
+// limit); an idle server admits it regardless, so no request waits forever
+// (submission refuses a request that alone exceeds either limit).
+inline bool admits(int64_t runningChains, int64_t runningBytes, int64_t C, int64_t bytes,
+                   int64_t maxChains, int64_t maxBytes) {
+    if (runningChains == 0) return true;
+    return runningChains + C <= maxChains && (maxBytes == 0 || runningBytes + bytes <= maxBytes);
+}
+
 // One chain's spins (int8, >= 0 is +1) as ceil(n/32) words, bit v = spin +1;
 // every word is written (tail bits past n are 0).  Eight spins at a time:
 // byte k of m is 1 where spin k >= 0 (its sign bit clear), and multiplying

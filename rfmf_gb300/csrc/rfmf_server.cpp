@@ -51,6 +51,7 @@ struct Request {
     // launch class
     int dbytes = 1, fmt = kCsrGlobal, W = 1;
     bool s64 = false;
+    int64_t devBytes = 0;             // request_device_bytes: counted against max_device_bytes
     // device state (worker thread only)
     DevBuf dBits, dBest, dBetaEnd, dBetaVal, dPhaseP, dPhaseIters;
     int64_t slot0 = -1;               // first of C consecutive chain slots
@@ -120,6 +121,7 @@ struct rfmf_server {
     rfmf_context* ctx = nullptr;
     uint64_t window = 4096;
     int64_t maxChains = int64_t(1) << 20;
+    int64_t maxDeviceBytes = 0;        // 0: no limit
     rfmf_launch_config lc{};
     Clock::time_point t0;
 
@@ -130,6 +132,7 @@ struct rfmf_server {
     std::deque<ReqPtr> queue;
     std::map<uint64_t, ReqPtr> all;    // every request not yet released
     int64_t runningChains = 0;
+    int64_t runningBytes = 0;          // request_device_bytes of the admitted requests
     rfmf_server_stats stats{};
 
 
@@ -485,6 +488,7 @@ void worker_main(rfmf_server* s) {
             }
             s->running.clear();
             s->runningChains = 0;
+            s->runningBytes = 0;
             s->cvDone.notify_all();
         }
     }
@@ -498,10 +502,12 @@ void worker_loop(rfmf_server* s) {
             s->cvWork.wait(lk, [&] { return s->stop || !s->queue.empty() || !s->running.empty(); });
             if (s->stop) break;
             while (!s->queue.empty() &&
-                   (s->runningChains + s->queue.front()->C <= s->maxChains || s->runningChains == 0)) {
+                   admits(s->runningChains, s->runningBytes, s->queue.front()->C,
+                          s->queue.front()->devBytes, s->maxChains, s->maxDeviceBytes)) {
                 ReqPtr r = s->queue.front();
                 s->queue.pop_front();
                 s->runningChains += r->C;
+                s->runningBytes += r->devBytes;
                 admitNow.push_back(r);
             }
         }
@@ -512,6 +518,7 @@ void worker_loop(rfmf_server* s) {
             if (rc != RFMF_OK) {
                 release(s, *r);
                 s->runningChains -= r->C;
+                s->runningBytes -= r->devBytes;
                 fail_request(*r, rc, rfmf_last_error(), s->now());
                 s->cvDone.notify_all();
             } else {
@@ -555,6 +562,7 @@ void worker_loop(rfmf_server* s) {
                 }
                 s->running.clear();
                 s->runningChains = 0;
+                s->runningBytes = 0;
             }
             for (auto& h : harvested) {
                 Request& r = *h.first;
@@ -566,6 +574,7 @@ void worker_loop(rfmf_server* s) {
                 }
                 release(s, r);
                 s->runningChains -= r.C;
+                s->runningBytes -= r.devBytes;
                 s->running.erase(std::find(s->running.begin(), s->running.end(), h.first));
             }
             s->cvDone.notify_all();
@@ -601,6 +610,8 @@ static int rfmf_server_create_impl(rfmf_context* ctx, const rfmf_server_config* 
         if (cfg->window_sweeps) s->window = cfg->window_sweeps;
         if (cfg->max_chains < 0) return fail(RFMF_ERR_INVALID, "max_chains must be >= 0");
         if (cfg->max_chains) s->maxChains = cfg->max_chains;
+        if (cfg->max_device_bytes < 0) return fail(RFMF_ERR_INVALID, "max_device_bytes must be >= 0");
+        s->maxDeviceBytes = cfg->max_device_bytes;
         s->lc = cfg->launch;
     }
     const rfmf_launch_config& c = s->lc;
@@ -683,6 +694,11 @@ static int rfmf_submit_impl(rfmf_server* s, const rfmf_graph* g, int64_t nchains
     // worker, where building them would stall the launch windows.
     if (int rc = build_beta_cached(s->ctx, r->t0s.data(), nchains, static_cast<int64_t>(total), r->bt))
         return rc;
+    r->devBytes = request_device_bytes(nchains, r->words, static_cast<int64_t>(r->bt.end.size()),
+                                       static_cast<int64_t>(r->phaseP.size()));
+    if (s->maxDeviceBytes && r->devBytes > s->maxDeviceBytes)
+        return fail(RFMF_ERR_CAPACITY, "request needs %lld device bytes, above max_device_bytes %lld",
+                    static_cast<long long>(r->devBytes), static_cast<long long>(s->maxDeviceBytes));
 
     // launch class
     const rfmf_launch_config& c = s->lc;
