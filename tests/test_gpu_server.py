@@ -138,3 +138,29 @@ def test_shared_beta_tables_and_refusal_at_submit(rfmf, ctx):
     with pytest.raises(rfmf.RfmfError):
         srv.submit(dg, bad["init"], bad["t0s"], bad["phases"], bad["iters"], bad["solver"])
     srv.close()
+
+
+def test_server_device_byte_budget(rfmf, ctx):
+    """max_device_bytes: each request's own device state here is 20,832 bytes
+    (2 x 32 chains x 13 spin words, 1,200 beta runs x 12 bytes, two 16-byte
+    schedule buffers, 32 chain records x 96 bytes), so under a 30,000-byte
+    budget the requests run one at a time, and each still equals its
+    standalone anneal; a request whose state alone exceeds the budget (two t0
+    tables: 35,232 bytes) is refused at submission."""
+    g = rfmf.erdos_renyi(400, 0.04, signed=True, seed=8)
+    dg = rfmf.DeviceGraph(ctx, g)
+    srv = rfmf.Server(ctx, window_sweeps=500, max_device_bytes=30000)
+    reqs = [_request(rfmf, g, list(range(2000 + 32 * k, 2032 + 32 * k)), [35.0 + k] * 32,
+                     [32, 1], [600, 600]) for k in range(3)]
+    ids = [srv.submit(dg, r["init"], r["t0s"], r["phases"], r["iters"], r["solver"]) for r in reqs]
+    sts = [srv.wait(rid, timeout=300) for rid in ids]
+    spans = sorted((s["start_s"], s["finish_s"]) for s in sts)
+    for (a0, a1), (b0, b1) in zip(spans, spans[1:]):
+        assert b0 >= a1 - 1e-9
+    for rid, r in zip(ids, reqs):
+        _same(srv.result(rid), _standalone(rfmf, ctx, dg, r))
+    two = _request(rfmf, g, list(range(3000, 3032)), [35.0, 36.0] * 16, [32, 1], [600, 600])
+    with pytest.raises(rfmf.RfmfError) as ei:
+        srv.submit(dg, two["init"], two["t0s"], two["phases"], two["iters"], two["solver"])
+    assert ei.value.code == 4
+    srv.close()
