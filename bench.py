@@ -408,10 +408,12 @@ def gpu_arm(args, rank, world):
             "items": info["items"],
             "balanced_items": bool(info["balanced"]),
             "score_path": "int64" if info["score64"] else "int32",
+            "launch_classes": info.get("launch_classes"),
             "l2": "flushed (256 MB write) between timed steps",
             "parallelism": f"replicas x{world}",
         },
-        "gpu_launches": K,
+        # one launch per launch class per timed step
+        "gpu_launches": K * max(1, int(info.get("launch_classes", 1))),
         "e2e": e2e,
         "plain_kernel": plain,
         "time_to_target": tt,
