@@ -362,6 +362,7 @@ def gpu_arm(args, rank, world):
         for e in tt:
             e["plain_seconds_est"] = e["sweeps"] * len(graphs) * args.chains / plain["value"]
     batched = None if args.no_batched else batched_arm(args, ctx)
+    ingest = ingest_arm(args, ctx, graphs, setup) if args.ingest else None
     serving = None
     if not args.no_serving:
         rates = [float(x) for x in str(args.serve_rate).split(",") if x]
@@ -419,6 +420,7 @@ def gpu_arm(args, rank, world):
         "time_to_target": tt,
         "batched": batched,
         "serving": serving,
+        "ingest_output": ingest,
         "clocks": clk,
         "roofline": {
             "bound": "smem",
@@ -499,6 +501,88 @@ def plain_kernel_arm(graphs, setup, sweeps, ctx):
             "identical_results": True,
             "what": "reference mcKernel compiled from its sources for sm_103a, kernel-only "
                     "cudaEvent time, one graph per launch as the reference runs"}
+
+
+def _median_time(fn, reps=3):
+    fn()
+    ts = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        out = fn()
+        ts.append(time.perf_counter() - t)
+    return statistics.median(ts), out
+
+
+def ingest_arm(args, ctx, graphs, setup):
+    """Graph ingest and output path, each against its host equivalent.
+
+    Ingest: rfmf_graph_from_edges (edge list in host memory -> CSR built on the
+    device: dense ids, degree count, scatter, row sort, dedupe, compact
+    formats) against graphs.csr_from_edges (numpy, one core) on the large
+    sparse shapes plus an Erdos-Renyi n = 20000 mean degree 48 graph, edges
+    in shuffled order; the two CSRs must be equal.  Output: rfmf_batch_cuts
+    (every chain's cut recomputed on the device) and rfmf_batch_partitions
+    (the '0'/'1' partition strings) for the 2048 chains of the bench workload
+    after 1000 sweeps, against rfmf_cut_value per chain and numpy strings on
+    the host; the results must be equal.  Wall times (median of 3 after one
+    warm-up call) of the public calls, host<->device copies included."""
+    import rfmf_gb300 as R
+    rng = np.random.default_rng(23)
+    ing = []
+    for g in (R.torus(100, 200, signed=True, seed=0, name="torus100x200"),
+              R.random_tree(10000, seed=0, name="tree10000"),
+              R.erdos_renyi_sparse(5000, 5, signed=True, seed=0, name="er5000_d5"),
+              R.erdos_renyi_degree(20000, 48, signed=True, seed=0, name="er20000_d48")):
+        rows = np.repeat(np.arange(g.n), np.diff(g.offsets.astype(np.int64)))
+        up = g.col > rows
+        u, v, w = rows[up], g.col[up].astype(np.int64), g.weight[up].astype(np.int64)
+        perm = rng.permutation(len(u))
+        u, v, w = u[perm], v[perm], w[perm]
+        t_dev, dg = _median_time(lambda: R.DeviceGraph.from_edges(ctx, u, v, w))
+        t_host, hg = _median_time(lambda: R.csr_from_edges(u, v, w))
+        off, col, wt = dg.csr()
+        same = (np.array_equal(off, hg.offsets) and np.array_equal(col, hg.col) and
+                np.array_equal(wt, hg.weight))
+        dg.close()
+        if not same:
+            raise AssertionError(f"device CSR of {g.name} differs from the host build")
+        ing.append({"graph": g.name, "n": g.n, "edges": int(len(u)), "device_ms": t_dev * 1e3,
+                    "host_numpy_ms": t_host * 1e3, "device_edges_per_s": len(u) / t_dev,
+                    "speedup": t_host / t_dev})
+
+    dgs = [R.DeviceGraph(ctx, s["g"]) for s in setup]
+    gl, ini, sol, t0 = [], [], [], []
+    for k, s in enumerate(setup):
+        gl += [dgs[k]] * len(s["seeds"])
+        ini += list(s["init"])
+        sol += s["solver"]
+        t0 += s["t0s"]
+    b = R.Batch(ctx, gl, t0, sol, ini, list(PHASES), [125] * len(PHASES))
+    b.run(1000)
+    out = b.read()
+    C = len(ini)
+    t_cut_dev, cuts = _median_time(lambda: b.cuts(best=False))
+    t_par_dev, parts = _median_time(lambda: b.partitions(best=False))
+    owners = [s["g"] for s in setup for _ in s["seeds"]]
+    t_cut_host, hcuts = _median_time(
+        lambda: np.array([R.cut_value(g, sp) for g, sp in zip(owners, out["end_spins"])]))
+    t_par_host, hparts = _median_time(
+        lambda: [np.where(sp > 0, ord("1"), ord("0")).astype(np.uint8).tobytes().decode()
+                 for sp in out["end_spins"]])
+    if not (np.array_equal(cuts, hcuts) and parts == hparts):
+        raise AssertionError("device output path differs from the host recompute")
+    b.close()
+    for d in dgs:
+        d.close()
+    nsum = sum(len(p) for p in parts)
+    return {"ingest": ing,
+            "output": {"chains": C, "vertices_total": nsum,
+                       "cuts_device_ms": t_cut_dev * 1e3, "cuts_host_ms": t_cut_host * 1e3,
+                       "partitions_device_ms": t_par_dev * 1e3,
+                       "partitions_host_ms": t_par_host * 1e3},
+            "what": "wall time of the public calls (median of 3 after a warm-up), host<->device "
+                    "copies included; host: numpy CSR build, rfmf_cut_value per chain, numpy "
+                    "strings; results equal"}
 
 
 def batched_graphs(count, seed=0):
@@ -759,6 +843,8 @@ def main():
     ap.add_argument("--batched-graphs", type=int, default=512)
     ap.add_argument("--batched-sweeps", type=int, default=2000)
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--ingest", action="store_true",
+                    help="also time graph ingest and the output path against their host equivalents")
     ap.add_argument("--serve-rate", default="2,10,100,2000",
                     help="req/s; a comma list sweeps several rates")
     ap.add_argument("--serve-seconds", type=float, default=20.0,
