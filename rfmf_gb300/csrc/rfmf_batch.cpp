@@ -327,6 +327,7 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
     if (c.gain_width != 0 && c.gain_width != 1 && c.gain_width != 4)
         return fail(RFMF_ERR_INVALID, "gain_width must be 0, 1 or 4");
     if (c.csr_format < 0 || c.csr_format > 3) return fail(RFMF_ERR_INVALID, "csr_format must be 0..3");
+    if (c.score_path < 0 || c.score_path > 2) return fail(RFMF_ERR_INVALID, "score_path must be 0..2");
     const int64_t totalAll = rfmf_total_steps(nphases, iters);   // src/host_common.cpp:196-210
     if (totalAll < 0) return fail(RFMF_ERR_CAPACITY, "iters total more than 10^12 sweeps");
     uint64_t total = 0, maxP = 0;
