@@ -793,8 +793,10 @@ static int rfmf_batch_partitions_impl(rfmf_batch* b, int which, char* out, int64
     for (int64_t n : b->chainN) maxN = std::max(maxN, n);
     if (stride < maxN) return fail(RFMF_ERR_INVALID, "stride %lld < largest n %lld", (long long)stride, (long long)maxN);
     if (int rc = rfmf_batch_synchronize(b)) return rc;
-    // chunks of chains bounded to ~256 MB of device staging
-    const int64_t per = std::max<int64_t>(1, std::min<int64_t>(b->C, (int64_t(256) << 20) / std::max<int64_t>(stride, 1)));
+    // chunks of chains bounded to ~256 MB of device staging and to 65535
+    // chains (one grid row per chain: gridDim.y is at most 65535)
+    const int64_t per = std::max<int64_t>(
+        1, std::min<int64_t>(std::min<int64_t>(b->C, 65535), (int64_t(256) << 20) / std::max<int64_t>(stride, 1)));
     DevBuf d;
     if (int rc = d.alloc(static_cast<size_t>(per * stride))) return rc;
     for (int64_t c0 = 0; c0 < b->C; c0 += per) {
