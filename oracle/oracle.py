@@ -1,7 +1,7 @@
 """ctypes bindings for the oracle library (oracle/_build/librfmf_oracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline leg as the checker.  The product never imports it.
+bench.py's CPU-baseline leg, as the oracle.  The product never imports it.
 """
 import ctypes as ct
 import os

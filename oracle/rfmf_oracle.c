@@ -1,8 +1,8 @@
 /*
  * rfmf_oracle.c -- CPU restatement of the RFMF annealer (gt-tinker/rfmf).
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the GPU path and the timed CPU
- * baseline.  The product never links or calls it.  Written as plain serial C
+ * TEST INFRASTRUCTURE ONLY: the oracle the GPU path is compared against and
+ * the timed CPU baseline.  The product never links or calls it.  Written as plain serial C
  * from the reference's algorithm; each function cites the reference lines it
  * restates.  Parity is pinned (see rfmf_oracle.h).
  */

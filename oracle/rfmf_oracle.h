@@ -2,7 +2,7 @@
  * rfmf_oracle.h -- CPU restatement of the RFMF annealer.
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product (rfmf_gb300/, include/)
- * links, loads or calls this library.  It is the checker that the GPU path is
+ * links, loads or calls this library.  It is the oracle that the GPU path is
  * compared against, and the CPU baseline that bench.py times beside it.
  *
  * Every function restates one piece of the reference (gt-tinker/rfmf); the
