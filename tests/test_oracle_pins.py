@@ -1,8 +1,10 @@
-"""The oracle (CPU restatement) pinned against the reference's own host code.
+"""The oracle (CPU restatement) pinned against the reference's own host code
+and against recorded runs of the reference's own GPU kernel.
 
 Fixtures in tests/golden/ were produced by tests/golden/make_golden.py from
 the reference's sources (oracle/_ref); where oracle/_ref is present the same
-checks also run live against it.
+checks also run live against it.  tests/golden/refkernel_runs.json holds runs
+of the reference's mcKernel on a GB300, which the oracle reproduces here.
 """
 import json
 
@@ -85,3 +87,37 @@ def test_committed_log_gpu_pin_record():
     for e in rec["gpu_entries"]:
         assert e["match"], e
         assert e["gpu"] == e["expected"]
+
+
+def _refkernel_cases():
+    import json
+    p = GOLDEN / "refkernel_runs.json"
+    cases = json.loads(p.read_text())["cases"] if p.exists() else []
+    # every recorded case (chains x sweeps x n up to 2e9: seconds on a few cores)
+    return [c for c in cases
+            if len(c["seeds"]) * sum(i for P, i in zip(c["phases"], c["iters"]) if P) * c["n"] <= 2e9]
+
+
+@pytest.mark.parametrize("case", _refkernel_cases(), ids=lambda c: c["name"])
+def test_oracle_reproduces_reference_kernel_runs(oracle, case):
+    """The oracle against the reference's own GPU kernel: runs of mcKernel
+    (its sources built for sm_103a, launched with the reference host code's
+    choices on a GB300; tests/golden/make_refkernel_golden.py) recorded best
+    and final cuts and partition digests, which the oracle must reproduce
+    exactly on the same graph, seeds and schedule."""
+    import hashlib
+    import sys
+
+    from conftest import ROOT, chains_for
+    sys.path.insert(0, str(ROOT / "tests" / "golden"))
+    import make_refkernel_golden as M
+
+    g = M.build_graph(case["graph"] if case["graph"] == "weighted300" else tuple(case["graph"]))
+    assert hashlib.sha256(g.offsets.tobytes() + g.col.tobytes() +
+                          g.weight.tobytes()).hexdigest() == case["csr_sha256"]
+    init, solver = chains_for(g, case["seeds"])
+    r = oracle.anneal(g, init, case["t0s"], solver, case["phases"], case["iters"])
+    assert [int(x) for x in r["best_vals"]] == case["best"]
+    assert [int(x) for x in r["cur_vals"]] == case["final"]
+    assert [M.psha(x) for x in r["best_spins"]] == case["best_partition_sha256"]
+    assert [M.psha(x) for x in r["end_spins"]] == case["final_partition_sha256"]
