@@ -16,7 +16,7 @@ import math
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, chains_for
+from conftest import GOLDEN, REFERENCE, chains_for
 
 LUT = [round(-math.log(-math.log((2 * i + 1) / 32)) * 2**20) for i in range(16)]
 
@@ -164,3 +164,36 @@ def test_anneal_fixtures(rfmf, oracle):
         assert [int(x) for x in r["cur_vals"]] == case["final"]
         assert [partition_sha(x) for x in r["best_spins"]] == case["best_partition_sha256"]
         assert [partition_sha(x) for x in r["end_spins"]] == case["final_partition_sha256"]
+
+
+@pytest.mark.skipif(not (REFERENCE / "Gset").exists(), reason="Gset files not present")
+def test_cut_consistency_all_gset(rfmf, oracle):
+    """tests/test_cut_consistency.sh:25-100 on the oracle: every Gset instance
+    (71 files), three chains (seeds 42, 43, 42; t0 105, 105, 90; phases
+    64..1 with 120 sweeps each); the tracked best and final cuts equal the
+    int64 recompute of the best and end spins; on the reference's sample set
+    each chain run alone equals it among the others.  Graphs come through the
+    native parser (rfmf_gset_parse) and the canonical CSR build."""
+    import re
+
+    names = sorted((p.name for p in (REFERENCE / "Gset").iterdir() if re.fullmatch(r"G\d+", p.name)),
+                   key=lambda s: int(s[1:]))
+    assert len(names) == 71
+    phases, iters = [64, 32, 16, 8, 4, 2, 1], [120] * 7
+    seeds, t0s = [42, 43, 42], [105.0, 105.0, 90.0]
+    for name in names:
+        e = rfmf.parse_gset(REFERENCE / "Gset" / name)
+        g = rfmf.csr_from_edges(e["u"], e["v"], e["w"], name=name)
+        init, solver = chains_for(g, seeds)
+        r = oracle.anneal(g, init, t0s, solver, phases, iters)
+        for c in range(3):
+            assert r["best_vals"][c] == g.cut_value(r["best_spins"][c]), name
+            assert r["cur_vals"][c] == g.cut_value(r["end_spins"][c]), name
+        if name in ("G1", "G11", "G22", "G63", "G70", "G81"):
+            # tests/test_chain_isolation.sh on the reference's sample set: a
+            # chain run alone equals the same chain among the others
+            for c in range(3):
+                one = oracle.anneal(g, init[c:c + 1], t0s[c:c + 1], solver[c:c + 1], phases, iters)
+                assert np.array_equal(one["end_spins"][0], r["end_spins"][c]), name
+                assert np.array_equal(one["best_spins"][0], r["best_spins"][c]), name
+                assert one["best_vals"][0] == r["best_vals"][c], name
