@@ -1022,7 +1022,9 @@ extern "C" int rfmf_anneal(rfmf_context* ctx, const rfmf_graph* g, int64_t max_w
                            int8_t* end_spins, int8_t* best_spins, float* kernel_ms,
                            int64_t* kernel_best_vals, int64_t* kernel_final_vals) {
     try {
-        return rfmf_anneal_impl(ctx, g, max_weighted_deg, C, initial_spins, t0s, nphases, phases, iters, solver_seeds, cfg, end_spins, best_spins, kernel_ms, kernel_best_vals, kernel_final_vals);
+        return rfmf_anneal_impl(ctx, g, max_weighted_deg, C, initial_spins, t0s, nphases, phases,
+                                iters, solver_seeds, cfg, end_spins, best_spins, kernel_ms,
+                                kernel_best_vals, kernel_final_vals);
     } catch (const std::bad_alloc&) {
         return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_anneal");
     } catch (...) {

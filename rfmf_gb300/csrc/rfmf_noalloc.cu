@@ -313,7 +313,10 @@ extern "C" int rfmf_anneal_noalloc(int device, void* stream, int64_t n,
                                    uint32_t* d_spin_bits, uint32_t* d_best_bits,
                                    int64_t* d_cur, int64_t* d_best) {
     try {
-        return rfmf_anneal_noalloc_impl(device, stream, n, d_offsets, d_edges, max_weighted_deg, C, t0s, solver_seeds, nphases, phases, iters, d_beta_end, d_beta_val, chain_beta_off, chain_beta_runs, d_spin_bits, d_best_bits, d_cur, d_best);
+        return rfmf_anneal_noalloc_impl(device, stream, n, d_offsets, d_edges, max_weighted_deg, C,
+                                        t0s, solver_seeds, nphases, phases, iters, d_beta_end,
+                                        d_beta_val, chain_beta_off, chain_beta_runs, d_spin_bits,
+                                        d_best_bits, d_cur, d_best);
     } catch (const std::bad_alloc&) {
         return rfmf::set_last_error(RFMF_ERR_NOMEM, "host allocation failed in rfmf_anneal_noalloc");
     } catch (...) {
