@@ -119,6 +119,10 @@ def test_csr_validation(rfmf):
     assert validate(rfmf, 2, [0, 1, 2], [1, 0], [0, 0])[0] == 1      # zero weight
     assert validate(rfmf, 2, [1, 1, 2], [1, 0], [1, 1])[0] == 1      # offsets[0] != 0
     assert validate(rfmf, 0, [0], [], [])[0] == 0                    # empty graph
+    assert validate(rfmf, 2, [0, 2, 4], [1, 1, 0, 0], [1, 1, 1, 1])[0] == 1   # duplicate entry
+    assert validate(rfmf, 3, [0, 2, 1, 4], [1, 2, 0, 0], [1, 1, 1, 1])[0] == 1  # offsets decrease
+    assert validate(rfmf, 2, [0, 1, 2], [1, 0], [2**31 - 1] * 2) == (0, 2**31 - 1)  # int32 max
+    assert validate(rfmf, 2, [0, 1, 2], [1, 0], [-2**31] * 2)[0] == 4  # |w| beyond int32
     L = rfmf.lib()
     h = ct.c_void_p()
     assert L.rfmf_graph_create(None, 2, None, None, None, ct.byref(h)) == 1
