@@ -352,7 +352,16 @@ def gpu_arm(args, rank, world):
     # e2e through the drop-in call with host buffers
     e2e = None
     if not args.no_e2e:
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
         e2e = e2e_arm(args, ctx, graphs, setup, per_step)
+        if world > 1:
+            # whole job: every rank's chain-steps over the slowest rank's time
+            import torch.distributed as dist
+            el = torch.tensor([e2e["elapsed_s"]], dtype=torch.float64, device="cuda")
+            dist.all_reduce(el, op=dist.ReduceOp.MAX)
+            e2e["value"] = e2e["chain_steps"] * world / float(el.item())
     plain = None
     if not args.no_plain:
         plain = plain_kernel_arm(graphs, setup, args.plain_sweeps, ctx)
@@ -812,7 +821,8 @@ def e2e_arm(args, ctx, graphs, setup, per_step):
             assert res.best_vals[0] == g.cut_value(res.best_spins[0])
     el = time.perf_counter() - t
     chain_steps = K * sum(len(s["seeds"]) for s in setup) * per_step
-    return {"value": chain_steps / el, "unit": "chain-steps/s",
+    return {"value": chain_steps / el, "unit": "chain-steps/s", "elapsed_s": el,
+            "chain_steps": chain_steps,
             "h2d_bytes_per_step": h2d // K, "d2h_bytes_per_step": d2h // K,
             "api": "rfmf_graph_create + rfmf_anneal (annealGpu drop-in), host buffers, "
                    f"{per_step} sweeps per chain per call"}
@@ -890,7 +900,7 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
     res = gpu_arm(args, rank, world)
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and world == 1 and not args.no_cpu:
         rate, cores, sample, _ = cpu_rate(workload_graphs(), 1, 0, args.cpu_seconds)
         res["cpu_baseline"] = {"value": rate, "unit": "chain-steps/s", "cores": cores,
                                "kind": "port", "sample": sample}
