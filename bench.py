@@ -188,34 +188,54 @@ def profile_traffic():
 
 
 # --------------------------------------------------------------- CPU arms
-def cpu_rate(graphs, steps, warmup, target_s, rank_seed_base=0):
-    """Oracle on all host cores: one chain per core over a compressed schedule
-    (same phases, equal sweeps per phase) on the workload's graphs."""
+SOLVER_SEED_OFFSET = 0xC2B2AE3D27D4EB4F
+
+
+def _oracle():
+    """The oracle (the C restatement of the reference's sweep): the CPU arms
+    use its own initial spins and nothing of librfmf.so."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as ora
-    import rfmf_gb300 as R
     ora.lib()
+    return ora
+
+
+def _cpu_chains(ora, g, seeds):
+    init = np.stack([ora.initial_spins(s, g.n) for s in seeds])
+    solver = [(int(s) + SOLVER_SEED_OFFSET) % 2**64 for s in seeds]
+    return init, solver
+
+
+def cpu_rate(graphs, steps, warmup, target_s, rank_seed_base=0):
+    """Oracle on all host cores: one chain per core over a compressed schedule
+    (same phases, equal sweeps per phase) on the workload's graphs.  Every
+    step's inputs are built before the clock starts."""
+    ora = _oracle()
     cores = ora.default_threads()
     # calibrate sweeps so one step takes ~target_s
     g0 = graphs[0]
+    init1, sol1 = _cpu_chains(ora, g0, [1])
     t = time.perf_counter()
-    ora.anneal(g0, R.initial_spins(1, g0.n)[None], [35.0], [R.solver_seed(1)], PHASES, [40] * 8,
-               nthreads=1)
+    ora.anneal(g0, init1, [35.0], sol1, PHASES, [40] * 8, nthreads=1)
     per_sweep = (time.perf_counter() - t) / 320 * (sum(g.n for g in graphs) / g0.n / len(graphs))
     # the two graphs run one after the other, each with one chain per core
     sweeps = max(800, int(target_s / 2 / max(per_sweep, 1e-7) / 8) * 8)
     nch = max(cores, 2)
     per_graph = [nch // 2, nch - nch // 2]
+    inputs = []
+    for step in range(warmup + steps):
+        row = []
+        for g, k in zip(graphs, per_graph):
+            seeds = [rank_seed_base + 10000 * step + i for i in range(k)]
+            init, solver = _cpu_chains(ora, g, seeds)
+            row.append((g, k, init, solver, [LADDER[i % 8] for i in range(k)]))
+        inputs.append(row)
     rates = []
     for step in range(warmup + steps):
         total_chain_sweeps = 0
         t = time.perf_counter()
-        for g, k in zip(graphs, per_graph):
-            seeds = [rank_seed_base + 10000 * step + i for i in range(k)]
-            init = np.stack([R.initial_spins(s, g.n) for s in seeds])
-            ora.anneal(g, init, [LADDER[i % 8] for i in range(k)],
-                       [R.solver_seed(s) for s in seeds], PHASES, [sweeps // 8] * 8,
-                       nthreads=cores)
+        for g, k, init, solver, t0s in inputs[step]:
+            ora.anneal(g, init, t0s, solver, PHASES, [sweeps // 8] * 8, nthreads=cores)
             total_chain_sweeps += k * sweeps
         el = time.perf_counter() - t
         if step >= warmup:
@@ -231,16 +251,12 @@ def cpu_config1(target_s):
     """The plain-method small case on the CPU restatement: ER n = 800, p = 0.06,
     +1 weights, 32 chains (raw seeds 0..31, t0 ladder), the default schedule
     compressed to a bounded sweep count, one chain per core."""
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle as ora
     import rfmf_gb300 as R
-    ora.lib()
+    ora = _oracle()
     cores = ora.default_threads()
     g = R.erdos_renyi(800, 0.06, seed=0, name="er800_p0.06")
-    seeds = list(range(32))
-    init = np.stack([R.initial_spins(x, g.n) for x in seeds])
+    init, sol = _cpu_chains(ora, g, list(range(32)))
     t0s = [LADDER[i % 8] for i in range(32)]
-    sol = [R.solver_seed(x) for x in seeds]
     t = time.perf_counter()
     ora.anneal(g, init[:cores], t0s[:cores], sol[:cores], PHASES, [64] * 8, nthreads=cores)
     per = (time.perf_counter() - t) / (512 * max(1, min(cores, 32) // cores))
@@ -373,10 +389,15 @@ def gpu_arm(args, rank, world):
     batched = None if args.no_batched else batched_arm(args, ctx)
     ingest = ingest_arm(args, ctx, graphs, setup) if args.ingest else None
     serving = None
+    serving_mixed = None
     if not args.no_serving:
         rates = [float(x) for x in str(args.serve_rate).split(",") if x]
         runs = [serving_arm(args, ctx, r) for r in rates]
         serving = runs[0] if len(runs) == 1 else runs
+        budgets = [int(float(x)) for x in str(args.serve_budgets).split(",") if x]
+        if budgets and args.serve_mixed_rate > 0:
+            serving_mixed = serving_arm(args, ctx, args.serve_mixed_rate, budgets=budgets,
+                                        max_requests=args.serve_mixed_requests)
 
     peaks = measured_peaks()
     sm_count = ctx.info()["sm_count"]
@@ -425,10 +446,9 @@ def gpu_arm(args, rank, world):
         # one launch per launch class per timed step
         "gpu_launches": K * max(1, int(info.get("launch_classes", 1))),
         "e2e": e2e,
-        "plain_kernel": plain,
         "time_to_target": tt,
-        "batched": batched,
         "serving": serving,
+        "serving_mixed_budgets": serving_mixed,
         "ingest_output": ingest,
         "clocks": clk,
         "roofline": {
@@ -448,6 +468,10 @@ def gpu_arm(args, rank, world):
         "issue_roofline": issue_roofline(traffic, value, sm_count, sm_mhz),
         "wall_s": wall,
         "step_ms": [round(m, 3) for m in step_ms],
+        # the >= 5x comparisons last: the plain one-graph-per-launch kernel
+        # (the reference's own) against the batched form on identical samples
+        "plain_kernel": plain,
+        "batched": batched,
     }
     return result
 
@@ -471,7 +495,10 @@ def plain_kernel_arm(graphs, setup, sweeps, ctx):
     """The reference's own kernel (one graph per launch, one block per chain,
     state in global memory), compiled from its sources for sm_103a and
     launched through oracle/refgpu.py, on a bounded sample of the same
-    workload; and librfmf.so's annealGpu drop-in on the identical sample."""
+    workload; against librfmf.so on the identical sample in two forms: the
+    batched form (both graphs' chains in one batch, one persistent launch)
+    and the annealGpu drop-in (one rfmf_anneal call per graph).  All three
+    must give identical results chain for chain."""
     sys.path.insert(0, str(ROOT / "oracle"))
     try:
         import refgpu
@@ -487,15 +514,16 @@ def plain_kernel_arm(graphs, setup, sweeps, ctx):
     ref_ms = ours_ms = 0.0
     cs = 0
     tpbs = []
-    for s in setup:
+    refs = []
+    dgs = [R.DeviceGraph(ctx, s["g"]) for s in setup]
+    for s, dg in zip(setup, dgs):
         g = s["g"]
         r = refgpu.run(g, s["init"], s["t0s"], s["solver"], phases, iters, sms)
+        refs.append(r)
         ref_ms += r["ms"]
         tpbs.append(r["tpb"])
-        dg = R.DeviceGraph(ctx, g)
         o = R.anneal_gpu(ctx, dg, g.max_weighted_degree(), s["init"], s["t0s"], phases, iters,
                          s["solver"])
-        dg.close()
         ours_ms += o.kernel_ms
         cs += len(s["seeds"]) * sweeps
         same = (np.array_equal(o.best_spins, r["best_spins"]) and
@@ -503,13 +531,38 @@ def plain_kernel_arm(graphs, setup, sweeps, ctx):
                 np.array_equal(o.best_vals, r["best_vals"]))
         if not same:
             raise AssertionError(f"reference kernel and librfmf.so differ on {g.name}")
-    return {"value": cs / (ref_ms / 1e3), "unit": "chain-steps/s",
-            "ours_same_sample": cs / (ours_ms / 1e3),
-            "sample": f"{len(setup)} launches (one per graph) x {len(setup[0]['seeds'])} chains x "
-                      f"{sweeps} sweeps (phases 128..1), threads/block {tpbs}",
+    gl, ini, sol, t0 = [], [], [], []
+    for s, dg in zip(setup, dgs):
+        gl += [dg] * len(s["seeds"])
+        ini += list(s["init"])
+        sol += s["solver"]
+        t0 += s["t0s"]
+    b = R.Batch(ctx, gl, t0, sol, ini, phases, iters)
+    batch_ms = b.run_timed(sweeps)
+    out = b.read()
+    b.close()
+    for d in dgs:
+        d.close()
+    c0 = 0
+    for s, r in zip(setup, refs):
+        C = len(s["seeds"])
+        if not (np.array_equal(np.stack(out["best_spins"][c0:c0 + C]), r["best_spins"]) and
+                np.array_equal(np.stack(out["end_spins"][c0:c0 + C]), r["end_spins"]) and
+                np.array_equal(out["best_vals"][c0:c0 + C], r["best_vals"])):
+            raise AssertionError(f"reference kernel and the batched form differ on {s['g'].name}")
+        c0 += C
+    plain = cs / (ref_ms / 1e3)
+    batched = cs / (batch_ms / 1e3)
+    dropin = cs / (ours_ms / 1e3)
+    return {"value": plain, "unit": "chain-steps/s",
+            "ours_batched": batched, "ours_dropin": dropin,
+            "speedup_vs_plain": batched / plain, "dropin_speedup_vs_plain": dropin / plain,
+            "sample": f"{len(setup)} graphs x {len(setup[0]['seeds'])} chains x {sweeps} sweeps "
+                      f"(phases 128..1); reference threads/block {tpbs}",
             "identical_results": True,
-            "what": "reference mcKernel compiled from its sources for sm_103a, kernel-only "
-                    "cudaEvent time, one graph per launch as the reference runs"}
+            "what": "reference mcKernel (its sources built for sm_103a), one launch per graph, "
+                    "kernel-only cudaEvent time; ours: both graphs in one batch (one launch), and "
+                    "rfmf_anneal per graph"}
 
 
 def _median_time(fn, reps=3):
@@ -620,12 +673,32 @@ def batched_graphs(count, seed=0):
     return out
 
 
+def _timed_graph_windows(ctx, batch, sweeps, window):
+    """Advance `batch` by `sweeps` sweeps as CUDA-graph replays of fixed
+    `window`-sweep launches (captured once before the clock), timed with
+    CUDA events on the library's stream."""
+    import torch
+    launches = max(1, sweeps // window)
+    assert launches * window == sweeps, "sweeps must be a multiple of the window"
+    batch.run_graph(window, launches, 0)          # capture + instantiate only
+    st = torch.cuda.ExternalStream(ctx.stream())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    batch.run_graph(window, launches, 1)
+    e1.record(st)
+    batch.synchronize()
+    return e0.elapsed_time(e1), launches
+
+
 def batched_arm(args, ctx):
-    """The batched form against the plain kernel on the same sample: G uneven
-    graphs x 64 chains in ONE persistent launch (work queue over graphs,
-    CTA shape and chains per CTA from the planner), vs the reference's kernel
-    launched once per graph as it runs.  Both advance every chain the same
-    sweeps; results must be identical chain for chain."""
+    """The batched form: G uneven graphs x 64 chains, all in one batch whose
+    sweeps run as CUDA-graph replays of fixed-size windows (work queue over
+    graphs, launch classes and chains per CTA from the planner).  Against the
+    plain kernel: the reference's kernel launched once per graph, as it runs,
+    on the first args.batched_plain_graphs graphs, with our batched form on
+    that same subset; both advance every chain the same sweeps and the
+    results must be identical chain for chain."""
     import torch
 
     import rfmf_gb300 as R
@@ -635,6 +708,7 @@ def batched_arm(args, ctx):
     gen_s = time.perf_counter() - t
     C = 64
     sweeps = args.batched_sweeps
+    window = args.batched_window
     phases, iters = schedule(sweeps)
     dgs = [R.DeviceGraph(ctx, g) for g in graphs]
     setup = []
@@ -643,26 +717,36 @@ def batched_arm(args, ctx):
         setup.append(dict(init=np.stack([R.initial_spins(x, g.n) for x in seeds]),
                           solver=[R.solver_seed(x) for x in seeds],
                           t0s=[LADDER[k % 8] for k in range(C)]))
-    gl, ini, sol, t0 = [], [], [], []
-    for dg, st in zip(dgs, setup):
-        gl += [dg] * C
-        ini += list(st["init"])
-        sol += st["solver"]
-        t0 += st["t0s"]
+
+    def make_batch(idx):
+        gl, ini, sol, t0 = [], [], [], []
+        for i in idx:
+            gl += [dgs[i]] * C
+            ini += list(setup[i]["init"])
+            sol += setup[i]["solver"]
+            t0 += setup[i]["t0s"]
+        return R.Batch(ctx, gl, t0, sol, ini, phases, iters)
+
+    every = list(range(len(graphs)))
     # warm-up batch (learned per-graph costs feed the work-item sizing)
-    wb = R.Batch(ctx, gl, t0, sol, ini, phases, iters)
+    wb = make_batch(every)
     wb.run_timed(min(sweeps, 2000))
     wb.close()
-    b = R.Batch(ctx, gl, t0, sol, ini, phases, iters)
-    ms = b.run_timed(sweeps)
+    b = make_batch(every)
+    ms, launches = _timed_graph_windows(ctx, b, sweeps, window)
     info = b.info()
-    out = b.read()
+    done = b.read()["sweeps_done"]
     b.close()
+    if not all(int(d) == sweeps for d in done):
+        raise AssertionError("batched form: not every chain finished its schedule")
     chain_steps = len(graphs) * C * sweeps
     res = {"value": chain_steps / (ms / 1e3), "unit": "chain-steps/s", "graphs": len(graphs),
-           "chains_per_graph": C, "sweeps": sweeps, "launches": 1, "kernel_ms": ms,
+           "chains_per_graph": C, "sweeps": sweeps, "window_sweeps": window,
+           "launch_windows": launches, "launches_per_window": info["launch_classes"],
+           "form": "CUDA-graph replay of fixed-size sweep windows", "kernel_ms": ms,
            "plan": {k: info[k] for k in ("threads_per_chain", "chains_per_cta", "grid", "items",
-                                         "csr_format", "gain_width", "balanced")},
+                                         "csr_format", "gain_width", "balanced",
+                                         "launch_classes")},
            "n_range": [min(g.n for g in graphs), max(g.n for g in graphs)],
            "graph_gen_s": gen_s}
     try:
@@ -673,25 +757,36 @@ def batched_arm(args, ctx):
     if not refgpu.available():
         res["plain_kernel"] = {"unavailable": "reference kernel cubin (oracle/_ref) not built"}
         return res
+    sub = every[:min(args.batched_plain_graphs, len(graphs))]
+    b = make_batch(sub)
+    ms_sub, _ = _timed_graph_windows(ctx, b, sweeps, window)
+    out = b.read()
+    b.close()
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     ref_ms = 0.0
     same = True
-    for i, (g, st) in enumerate(zip(graphs, setup)):
-        r = refgpu.run(g, st["init"], st["t0s"], st["solver"], phases, iters, sms)
+    for k, i in enumerate(sub):
+        st = setup[i]
+        r = refgpu.run(graphs[i], st["init"], st["t0s"], st["solver"], phases, iters, sms)
         ref_ms += r["ms"]
-        mine_best = np.stack(out["best_spins"][i * C:(i + 1) * C])
-        mine_end = np.stack(out["end_spins"][i * C:(i + 1) * C])
-        same = same and np.array_equal(mine_best, r["best_spins"]) and \
-            np.array_equal(mine_end, r["end_spins"]) and \
-            np.array_equal(out["best_vals"][i * C:(i + 1) * C], r["best_vals"])
-    plain = chain_steps / (ref_ms / 1e3)
-    res["plain_kernel"] = {"value": plain, "unit": "chain-steps/s", "launches": len(graphs),
-                           "kernel_ms": ref_ms, "identical_results": bool(same),
-                           "what": "reference mcKernel (sm_103a build of its sources), one "
-                                   "launch per graph, kernel-only cudaEvent time"}
-    res["speedup_vs_plain"] = res["value"] / plain
+        sl = slice(k * C, (k + 1) * C)
+        same = same and np.array_equal(np.stack(out["best_spins"][sl]), r["best_spins"]) and \
+            np.array_equal(np.stack(out["end_spins"][sl]), r["end_spins"]) and \
+            np.array_equal(out["best_vals"][sl], r["best_vals"])
+    for d in dgs:
+        d.close()
     if not same:
         raise AssertionError("batched results differ from the reference kernel")
+    cs_sub = len(sub) * C * sweeps
+    plain = cs_sub / (ref_ms / 1e3)
+    ours = cs_sub / (ms_sub / 1e3)
+    res["plain_kernel"] = {"value": plain, "unit": "chain-steps/s", "graphs": len(sub),
+                           "launches": len(sub), "kernel_ms": ref_ms, "ours_same_graphs": ours,
+                           "ours_kernel_ms": ms_sub, "identical_results": bool(same),
+                           "what": "reference mcKernel (sm_103a build of its sources), one "
+                                   "launch per graph, kernel-only cudaEvent time, on the first "
+                                   f"{len(sub)} graphs; ours on the same graphs in one batch"}
+    res["speedup_vs_plain"] = ours / plain
     return res
 
 
@@ -706,16 +801,18 @@ def serving_graphs():
     return out
 
 
-def serving_arm(args, ctx, rate):
+def serving_arm(args, ctx, rate, budgets=None, max_requests=None):
     """Continuous batching through the request server: Poisson arrivals at
-    `rate` req/s for `seconds`, or until args.serve_max_requests have
-    arrived (which bounds the high-rate runs: at 2000 req/s the cap's
-    requests arrive in a fraction of a second and the run measures the
-    saturated server); each request draws a graph from the large-sparse
-    families (torus, tree, ER d=5; n 5000-20000), 16-256 chains and a budget
-    of args.serve_sweeps sweeps (default schedule).  Latency = submit ->
-    results on the host (server clock).  `offered_rate_req_s` is the rate at
-    which the submitting thread actually handed requests to the server."""
+    `rate` req/s for `seconds`, or until max_requests (default
+    args.serve_max_requests) have arrived (which bounds the high-rate runs:
+    at 2000 req/s the cap's requests arrive in a fraction of a second and the
+    run measures the saturated server); each request draws a graph from the
+    large-sparse families (torus, tree, ER d=5; n 5000-20000), 16-256 chains
+    and a sweep budget (default schedule): args.serve_sweeps, or drawn
+    uniformly from `budgets` when given, so that short and long requests
+    share windows.  Latency = submit -> results on the host (server clock).
+    `offered_rate_req_s` is the rate at which the submitting thread actually
+    handed requests to the server."""
     import threading
 
     import rfmf_gb300 as R
@@ -725,15 +822,17 @@ def serving_arm(args, ctx, rate):
     seconds = args.serve_seconds
     arrivals = []
     t = 0.0
-    while len(arrivals) < args.serve_max_requests:
+    cap = max_requests or args.serve_max_requests
+    while len(arrivals) < cap:
         t += float(rng.exponential(1.0 / rate))
         if t > seconds:
             break
         arrivals.append(t)
     submitted = [0.0] * len(arrivals)
     reqs = [dict(g=int(rng.integers(len(graphs))), C=int(rng.choice([16, 32, 64, 128, 256])),
-                 seed0=10_000_000 + 1000 * i) for i in range(len(arrivals))]
-    phases, iters = schedule(args.serve_sweeps)
+                 seed0=10_000_000 + 1000 * i,
+                 sweeps=int(rng.choice(budgets)) if budgets else args.serve_sweeps)
+            for i in range(len(arrivals))]
     srv = R.Server(ctx, window_sweeps=args.serve_window)
     ids = [None] * len(reqs)
     err = []
@@ -757,6 +856,7 @@ def serving_arm(args, ctx, rate):
             if d > 0:
                 time.sleep(d)
             try:
+                phases, iters = schedule(r["sweeps"])
                 ids[i] = srv.submit(dgs[r["g"]], init, t0s, phases, iters, solver)
                 submitted[i] = time.perf_counter() - t0
             except Exception as e:   # pragma: no cover
@@ -770,16 +870,18 @@ def serving_arm(args, ctx, rate):
     if err:
         raise RuntimeError(err[0])
     lat, cs = [], 0
+    lat_by_budget = {}
     for i, r in enumerate(reqs):
         st = srv.wait(ids[i], timeout=600)
         if st["state"] != "done":
             raise RuntimeError(f"request {i} {st['state']}")
         lat.append(st["finish_s"] - st["submit_s"])
+        lat_by_budget.setdefault(r["sweeps"], []).append(lat[-1])
         res = srv.result(ids[i])
         g = graphs[r["g"]]
         if res.best_vals[0] != g.cut_value(res.best_spins[0]):
             raise AssertionError("served best cut disagrees with its spins")
-        cs += r["C"] * args.serve_sweeps
+        cs += r["C"] * r["sweeps"]
     wall = time.perf_counter() - t_start
     stats = srv.stats()
     srv.close()
@@ -788,7 +890,11 @@ def serving_arm(args, ctx, rate):
     return {"rate_req_s": rate, "requests": len(reqs),
             "arrival_window_s": arrivals[-1] if arrivals else 0.0,
             "offered_rate_req_s": (len(submitted) - 1) / span if span > 0 else None,
-            "sweeps_per_request": args.serve_sweeps, "window_sweeps": args.serve_window,
+            "sweeps_per_request": sorted(set(r["sweeps"] for r in reqs)),
+            "window_sweeps": args.serve_window,
+            "latency_by_budget": {str(k): {"requests": len(v), "p50_s": float(np.percentile(v, 50)),
+                                           "p99_s": float(np.percentile(v, 99))}
+                                  for k, v in sorted(lat_by_budget.items())},
             "latency_p50_s": float(np.percentile(lat, 50)),
             "latency_p99_s": float(np.percentile(lat, 99)),
             "latency_max_s": float(lat.max()),
@@ -800,18 +906,30 @@ def serving_arm(args, ctx, rate):
 
 
 def e2e_arm(args, ctx, graphs, setup, per_step):
+    """End to end through the drop-in: per step and graph, rfmf_graph_create
+    (host CSR -> device) and one rfmf_anneal call (host spins in, host spins
+    and cuts out), all inside the clock.  The breakdown splits the wall time
+    into graph upload, the annealing kernel's own device time, and the rest of
+    each rfmf_anneal call (beta tables, batch set-up and copies, read-back)."""
     import rfmf_gb300 as R
     phases, iters = schedule(per_step)
     K = min(args.steps, 2)
     h2d = d2h = 0
+    t_graph = t_call = kern = 0.0
     t = time.perf_counter()
     for _ in range(K):
         for s in setup:
             g = s["g"]
+            t1 = time.perf_counter()
             dg = R.DeviceGraph(ctx, g)
+            t2 = time.perf_counter()
             res = R.anneal_gpu(ctx, dg, g.max_weighted_degree(), s["init"], s["t0s"], phases,
                                iters, s["solver"])
+            t3 = time.perf_counter()
             dg.close()
+            t_graph += t2 - t1
+            t_call += t3 - t2
+            kern += res.kernel_ms / 1e3
             C = len(s["seeds"])
             words = (g.n + 31) // 32
             runs = len(R.beta_tables(sorted(set(s["t0s"])), per_step)[0])
@@ -824,8 +942,12 @@ def e2e_arm(args, ctx, graphs, setup, per_step):
     return {"value": chain_steps / el, "unit": "chain-steps/s", "elapsed_s": el,
             "chain_steps": chain_steps,
             "h2d_bytes_per_step": h2d // K, "d2h_bytes_per_step": d2h // K,
-            "api": "rfmf_graph_create + rfmf_anneal (annealGpu drop-in), host buffers, "
-                   f"{per_step} sweeps per chain per call"}
+            "breakdown_s": {"graph_upload": t_graph, "anneal_kernel": kern,
+                            "anneal_call_other": t_call - kern,
+                            "outside_calls": el - t_graph - t_call},
+            "kernel_only_rate": chain_steps / kern,
+            "api": "rfmf_graph_create + rfmf_anneal (annealGpu drop-in), host buffers, one call "
+                   f"per graph, {per_step} sweeps per chain per call"}
 
 
 def main():
@@ -851,7 +973,11 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-graphs", type=int, default=512)
-    ap.add_argument("--batched-sweeps", type=int, default=2000)
+    ap.add_argument("--batched-sweeps", type=int, default=20000)
+    ap.add_argument("--batched-window", type=int, default=2500,
+                    help="sweeps per CUDA-graph window of the batched form")
+    ap.add_argument("--batched-plain-graphs", type=int, default=128,
+                    help="graphs of the batched mix also run on the plain kernel")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--ingest", action="store_true",
                     help="also time graph ingest and the output path against their host equivalents")
@@ -863,6 +989,11 @@ def main():
                     help="arrivals per rate at most (bounds the high-rate runs)")
     ap.add_argument("--serve-sweeps", type=int, default=100_000)
     ap.add_argument("--serve-window", type=int, default=4096)
+    ap.add_argument("--serve-budgets", default="100000,1000000",
+                    help="sweep budgets mixed in one serving run (10^7 adds minutes of wall time)")
+    ap.add_argument("--serve-mixed-rate", type=float, default=10.0,
+                    help="req/s of the mixed-budget serving run (0 = skip)")
+    ap.add_argument("--serve-mixed-requests", type=int, default=40)
     args = ap.parse_args()
     if args.chains is None:
         args.chains = WORKLOAD_CHAINS[args.workload]
@@ -905,6 +1036,18 @@ def main():
         res["cpu_baseline"] = {"value": rate, "unit": "chain-steps/s", "cores": cores,
                                "kind": "port", "sample": sample}
         res["cpu_config1"] = cpu_config1(min(6.0, args.cpu_seconds))
+    # keep the plain-kernel comparisons at the end of the line, with a short
+    # summary after them
+    for k in ("plain_kernel", "batched"):
+        res[k] = res.pop(k, None)
+    pk, bt = res.get("plain_kernel") or {}, res.get("batched") or {}
+    res["vs_plain_kernel"] = {
+        "batched_same_sample": pk.get("speedup_vs_plain"),
+        "dropin_same_sample": pk.get("dropin_speedup_vs_plain"),
+        "batched_512_graph_mix": bt.get("speedup_vs_plain"),
+        "identical_results": bool(pk.get("identical_results") and
+                                  (bt.get("plain_kernel") or {}).get("identical_results")),
+    }
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

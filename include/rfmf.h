@@ -56,6 +56,21 @@ int rfmf_context_destroy(rfmf_context* ctx);
  * block).  Either pointer may be NULL. */
 int rfmf_context_info(const rfmf_context* ctx, int* sm_count, int* smem_optin);
 
+/* The context's CUDA stream (a cudaStream_t) in *stream: every launch and
+ * copy of the context's batches goes to it, so a caller can order its own
+ * work against them or time them with its own events.  No reference
+ * counterpart (the reference uses the default stream). */
+int rfmf_context_stream(const rfmf_context* ctx, void** stream);
+
+/* The context's device-resident beta run tables (one per (t0, sweeps) in
+ * use, shared by every batch, rfmf_anneal call and served request of the
+ * context; the reference builds and uploads a set per launch,
+ * src/host_common.cpp:277-294): *tables live now, *device_bytes they hold,
+ * *uploads performed since the context was created.  Any pointer may be
+ * NULL. */
+int rfmf_context_beta_cache(rfmf_context* ctx, int64_t* tables, int64_t* device_bytes,
+                            uint64_t* uploads);
+
 /*
  * Upload a CSR graph: n vertices, offsets[n+1], col/weight[offsets[n]].
  * Replaces the CSR flatten + upload of src/anneal_kernels.cu:666-741 (the
@@ -225,12 +240,6 @@ int rfmf_batch_stats(rfmf_batch* b, uint64_t* improved_sweeps);
 /* Wait for the batch's work; reports a device-side error if one occurred. */
 int rfmf_batch_synchronize(rfmf_batch* b);
 
-/* Testing aid for the failure path: overwrite chain `chain`'s carried cut
- * value on the device (after the batch's queued work).  The next launch
- * finds it inconsistent with the chain's spins and the batch reports
- * RFMF_ERR_DEVICE; the context stays usable.  No GPU fault is involved. */
-int rfmf_batch_debug_set_cut(rfmf_batch* b, int64_t chain, int64_t cut);
-
 /* Copy chain state to the host (synchronous).  Any pointer may be NULL.
  * end_spins/best_spins: concatenated like initial_spins. */
 int rfmf_batch_read(rfmf_batch* b, int8_t* end_spins, int8_t* best_spins,
@@ -341,35 +350,42 @@ int rfmf_server_stats_get(rfmf_server* s, rfmf_server_stats* out);
 /*
  * The annealer for callers that cannot allocate device memory.  No reference
  * counterpart: an addition for hosts whose allocator owns all device memory,
- * code that must not allocate (or synchronise) in the middle of its work, and
- * embedders that hand the library pre-sized buffers.  It allocates nothing:
- * inputs and outputs are the caller's device buffers, and the kernel's
- * scratch (chain records, work items, queue head, error word) lives in a
- * fixed 640 KiB file-scope device array that every GPU loading this library
- * holds until the process exits.
+ * code that must not allocate in the middle of its work, and embedders that
+ * hand the library pre-sized buffers.  It allocates nothing: inputs and
+ * outputs are the caller's device buffers, and the kernel's scratch (graph,
+ * schedule and chain records, work items, queue head, error word) lives in a
+ * fixed 476,672-byte (about 466 KiB) file-scope device array that every GPU
+ * loading this library holds until the process exits.
  *
  * Limits: C <= 4096 chains, nphases <= 64 (RFMF_ERR_CAPACITY beyond).
- * Inputs (device): d_offsets[n+1] (uint32), d_edges[2 * offsets[n]] as
- * {int32 col, int32 weight} pairs (the symmetric, row-sorted CSR that
- * rfmf_csr_validate accepts), d_beta_end / d_beta_val (the run tables of
- * rfmf_beta_tables for these t0s over the executed sweeps), d_spin_bits
- * (C * ceil(n/32) words, bit v of chain c = spin +1; overwritten with the
- * final spins).  Host: t0s, solver_seeds, phases, iters, chain_beta_off
- * (first run of each chain's table), chain_beta_runs (its run count), and
- * max_weighted_deg = the graph's true B.  Outputs (device): d_best_bits
- * (same layout), d_cur / d_best (C int64 each).  Synchronous on `stream`
- * (a cudaStream_t, NULL for the legacy default stream).  The first call on a
- * device looks up the array's address and should come before any stream
- * capture; the array is shared by all calls, which clear what they need, and
- * calls that overlap on the GPU race on it.
+ * Inputs (device): d_offsets[n+1] (uint32, 4-byte aligned), d_edges[2 *
+ * offsets[n]] as {int32 col, int32 weight} pairs (8-byte aligned; the
+ * symmetric, row-sorted CSR that rfmf_csr_validate accepts), d_beta_end /
+ * d_beta_val (8- / 4-byte aligned: the beta_runs runs of rfmf_beta_tables
+ * for these t0s over the executed sweeps), d_spin_bits (4-byte aligned,
+ * C * ceil(n/32) words, bit v of chain c = spin +1; overwritten with the final
+ * spins).  Host: t0s, solver_seeds, phases, iters, chain_beta_off (first run
+ * of each chain's table), chain_beta_runs (its run count; off + runs <=
+ * beta_runs), and max_weighted_deg = a bound on every row's sum of |w|.
+ * Outputs (device): d_best_bits (same layout), d_cur / d_best (C int64 each,
+ * 8-byte aligned).  The CSR is checked on the device before the anneal; one
+ * that breaks the invariants or the bound gives RFMF_ERR_INVALID without
+ * annealing (outputs then unspecified).  Misaligned pointers give
+ * RFMF_ERR_INVALID before any device work.  Synchronous on `stream` (a
+ * cudaStream_t, NULL for the legacy default stream): it returns once the
+ * anneal has finished.  The first call on a device looks up the array's
+ * address and should come before any stream capture; the array is shared by
+ * all calls, which clear what they need, and calls that overlap on the GPU
+ * race on it.
  */
 int rfmf_anneal_noalloc(int device, void* stream, int64_t n, const uint32_t* d_offsets,
                         const int32_t* d_edges, int64_t max_weighted_deg, int64_t C,
                         const double* t0s, const uint64_t* solver_seeds, int64_t nphases,
                         const uint64_t* phases, const uint64_t* iters, const int64_t* d_beta_end,
-                        const int32_t* d_beta_val, const int64_t* chain_beta_off,
-                        const int64_t* chain_beta_runs, uint32_t* d_spin_bits,
-                        uint32_t* d_best_bits, int64_t* d_cur, int64_t* d_best);
+                        const int32_t* d_beta_val, int64_t beta_runs,
+                        const int64_t* chain_beta_off, const int64_t* chain_beta_runs,
+                        uint32_t* d_spin_bits, uint32_t* d_best_bits, int64_t* d_cur,
+                        int64_t* d_best);
 
 #ifdef __cplusplus
 }

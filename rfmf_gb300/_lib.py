@@ -15,13 +15,16 @@ _I64 = ct.c_int64
 _U64 = ct.c_uint64
 _I32 = ct.c_int32
 
-# (name, restype, argtypes) for every symbol include/rfmf.h declares.
+# (name, restype, argtypes) for every symbol the C headers (include/rfmf.h and
+# the testing aids of include/rfmf_testing.h) declare.
 SIGNATURES = [
     ("rfmf_version", ct.c_char_p, []),
     ("rfmf_last_error", ct.c_char_p, []),
     ("rfmf_context_create", ct.c_int, [ct.c_int, _P]),
     ("rfmf_context_destroy", ct.c_int, [_P]),
     ("rfmf_context_info", ct.c_int, [_P, _P, _P]),
+    ("rfmf_context_stream", ct.c_int, [_P, _P]),
+    ("rfmf_context_beta_cache", ct.c_int, [_P, _P, _P, _P]),
     ("rfmf_graph_create", ct.c_int, [_P, _I64, _P, _P, _P, _P]),
     ("rfmf_graph_destroy", ct.c_int, [_P]),
     ("rfmf_csr_validate", ct.c_int, [_I64, _P, _P, _P, _P]),
@@ -46,7 +49,7 @@ SIGNATURES = [
     ("rfmf_batch_info", ct.c_int, [_P, _P]),
     ("rfmf_batch_destroy", ct.c_int, [_P]),
     ("rfmf_anneal_noalloc", ct.c_int, [ct.c_int, _P, _I64, _P, _P, _I64, _I64, _P, _P, _I64,
-                                       _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+                                       _P, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _P]),
     ("rfmf_gset_header", ct.c_int, [ct.c_char_p, ct.c_size_t, _P, _P]),
     ("rfmf_gset_parse", ct.c_int, [ct.c_char_p, ct.c_size_t, ct.c_double, _I64, _P, _P, _P, _P,
                                    _P, _P]),

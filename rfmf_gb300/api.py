@@ -129,6 +129,19 @@ class Context:
         check(lib().rfmf_context_info(self.h, ct.byref(sms), ct.byref(smem)))
         return dict(sm_count=sms.value, smem_optin=smem.value)
 
+    def stream(self):
+        """The context's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+        p = ct.c_void_p()
+        check(lib().rfmf_context_stream(self.h, ct.byref(p)))
+        return p.value or 0
+
+    def beta_cache(self):
+        """Device-resident beta tables of the context: live tables, their
+        bytes, and uploads so far."""
+        t, b, u = ct.c_int64(), ct.c_int64(), ct.c_uint64()
+        check(lib().rfmf_context_beta_cache(self.h, ct.byref(t), ct.byref(b), ct.byref(u)))
+        return dict(tables=t.value, device_bytes=b.value, uploads=u.value)
+
     def close(self):
         if self.h:
             lib().rfmf_context_destroy(self.h)

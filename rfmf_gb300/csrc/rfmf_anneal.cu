@@ -1096,9 +1096,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* mbar, uint32_t parity) {
 }
 
 // Stage graph g's compact CSR into shared memory: thread 0 arms the mbarrier
-// with the byte count and issues the bulk copies (<= 64 KB each); everyone
-// waits on the phase with a bounded poll.  Returns false on timeout.
-__device__ bool stage_csr(const DevGraph& g, unsigned char* dst, uint64_t* mbar, uint32_t& phase) {
+// with the byte count and issues the bulk copies (<= 64 KB each); every
+// thread waits on the phase with a bounded poll.  Returns this thread's
+// outcome (false: its polls ran out); the caller makes it CTA-uniform and
+// advances the phase.
+__device__ bool stage_csr(const DevGraph& g, unsigned char* dst, uint64_t* mbar, uint32_t phase) {
     const uint32_t total = g.offBytes + g.entBytes;
     if (threadIdx.x == 0) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -1117,7 +1119,6 @@ __device__ bool stage_csr(const DevGraph& g, unsigned char* dst, uint64_t* mbar,
     }
     bool ok = false;
     for (int i = 0; i < kMaxCopyPolls && !ok; ++i) ok = mbar_try_wait(mbar, phase);
-    phase ^= 1u;
     return ok;
 }
 
@@ -1144,7 +1145,6 @@ __global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) 
 
     uint32_t phase = 0;
     int loaded = -1;
-    bool dead = false;
     for (;;) {
         if (threadIdx.x == 0) *sItem = atomicAdd(L.queue, 1);
         __syncthreads();
@@ -1164,13 +1164,23 @@ __global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) 
             csr.off = g.offsets;
             csr.ent = g.edges;
         } else {
-            if (item.graph != loaded && !dead) {
-                if (!stage_csr(g, csrBase, mbar, phase)) {
-                    // The copy may still be in flight: this CTA never touches
-                    // the region again; report and keep draining the queue.
-                    dead = true;
+            if (item.graph != loaded) {
+                // All threads agree on the outcome, so that a chain's
+                // barriers never see part of its warp group leave.
+                if (!__syncthreads_and(stage_csr(g, csrBase, mbar, phase))) {
+                    // The copy may still be in flight.  Report it, then stay
+                    // resident for a second, longer bounded wait: a CTA that
+                    // retired with a copy outstanding would leave its target
+                    // shared memory to whatever CTA the SM runs next.  The
+                    // CTA then takes no more work; the host reports the error
+                    // and the context is not to be reused.
                     if (threadIdx.x == 0) raise_error(L, kDevCopyTimeout, it);
+                    bool landed = false;
+                    for (int i = 0; i < 4 * kMaxCopyPolls && !landed; ++i) landed = mbar_try_wait(mbar, phase);
+                    __syncthreads();
+                    break;
                 }
+                phase ^= 1u;
                 loaded = item.graph;
             }
             csr.off = reinterpret_cast<const uint32_t*>(csrBase);
@@ -1180,7 +1190,7 @@ __global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) 
         if (threadIdx.x < 16) sProg[threadIdx.x] = (static_cast<int>(threadIdx.x) < active) ? 0 : INT_MAX;
         if (threadIdx.x == 0) sProg[16] = active;
         __syncthreads();
-        if (!dead && grp < active)
+        if (grp < active)
             run_chain<DP, kFmt, kS64>(L, cs, csr, lut, L.order[item.first + grp], t, T, grp);
         __syncthreads();
         if (threadIdx.x == 0 && L.itemNs) {

@@ -27,6 +27,7 @@
 #include <tuple>
 #include <vector>
 
+#include "../../include/rfmf_testing.h"
 #include "rfmf_host.h"
 
 using namespace rfmf;
@@ -62,7 +63,8 @@ struct rfmf_batch {
     std::vector<int64_t> graphOfChain;
     int64_t words = 0;                           // total spin words over chains
     std::vector<const rfmf_graph*> glist;
-    DevBuf dGraphs, dScheds, dChains, dPhaseP, dPhaseIters, dBetaEnd, dBetaVal, dBits, dBest;
+    DevBuf dGraphs, dScheds, dChains, dPhaseP, dPhaseIters, dBits, dBest;
+    std::vector<DevBetaRef> betaRefs;            // the context's shared beta tables in use
     std::vector<BatchClass> cls;
     cudaEvent_t fork = nullptr;
     uint64_t hostDone = 0;       // sweeps every chain has been advanced by
@@ -273,17 +275,24 @@ int harvest_item_times(rfmf_batch& b, BatchClass& k) {
 // One window: every class's launch.  A single class goes out on the
 // context's stream; several are forked onto their own streams and joined
 // back, so run_timed events and graph capture see the whole window.
+// Re-size the work items of classes not yet balanced, once every graph of
+// the class has a learned cost (stream-ordered after older launches).
+int rebalance(rfmf_batch* b) {
+    for (BatchClass& k : b->cls) {
+        if (k.balanced) continue;
+        plan_balanced(*b, k);
+        if (k.balanced) {
+            build_items(*b, k);
+            if (int rc = upload_items(*b, k)) return rc;
+        }
+    }
+    return RFMF_OK;
+}
+
 int enqueue_run(rfmf_batch* b, uint64_t sweeps, bool capturing = false) {
     cudaStream_t main = b->ctx->stream;
     if (!capturing) {
-        for (BatchClass& k : b->cls) {
-            if (k.balanced) continue;
-            plan_balanced(*b, k);
-            if (k.balanced) {
-                build_items(*b, k);
-                if (int rc = upload_items(*b, k)) return rc;   // stream-ordered after older launches
-            }
-        }
+        if (int rc = rebalance(b)) return rc;
         const uint64_t adv = std::min<uint64_t>(sweeps, b->total - std::min(b->total, b->hostDone));
         b->hostDone += adv;
         for (BatchClass& k : b->cls) k.pendingSweeps = adv;
@@ -551,10 +560,12 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
     }
     for (BatchClass& k : b->cls) build_items(*b, k);
 
-    // Beta tables over the executed sweeps.
-    BetaTables bt;
-    int rc = build_beta_cached(ctx, t0s, C, static_cast<int64_t>(total), bt);
+    // Beta tables over the executed sweeps: the context's device copies,
+    // shared with every other batch, call and request at the same (t0, sweeps).
+    ChainBeta cb;
+    int rc = acquire_beta(ctx, t0s, C, static_cast<int64_t>(total), cb);
     if (rc) return rc;
+    b->betaRefs = cb.refs;
 
     std::vector<DevGraph> hg(G);
     for (size_t gi = 0; gi < G; ++gi) {
@@ -594,8 +605,6 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
     if ((rc = b->dChains.alloc(C * sizeof(DevChain)))) return rc;
     if ((rc = b->dPhaseP.alloc(std::max<int64_t>(nphases, 1) * sizeof(uint32_t)))) return rc;
     if ((rc = b->dPhaseIters.alloc(std::max<int64_t>(nphases, 1) * sizeof(uint64_t)))) return rc;
-    if ((rc = b->dBetaEnd.alloc(bt.end.size() * sizeof(int64_t)))) return rc;
-    if ((rc = b->dBetaVal.alloc(bt.val.size() * sizeof(int32_t)))) return rc;
     if ((rc = b->dBits.alloc(bits.size() * sizeof(uint32_t)))) return rc;
     if ((rc = b->dBest.alloc(bits.size() * sizeof(uint32_t)))) return rc;
     for (BatchClass& k : b->cls) {
@@ -622,9 +631,9 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
         d.graph = static_cast<int32_t>(b->graphOfChain[i]);
         d.sched = 0;
         d.solverSeed = solver_seeds[i];
-        d.betaEnd = b->dBetaEnd.as<int64_t>() + bt.chainOff[i];
-        d.betaVal = b->dBetaVal.as<int32_t>() + bt.chainOff[i];
-        d.betaRuns = bt.chainRuns[i];
+        d.betaEnd = cb.end[i];
+        d.betaVal = cb.val[i];
+        d.betaRuns = cb.runs[i];
         d.spinBits = b->dBits.as<uint32_t>() + b->chainWordOff[i];
         d.bestBits = b->dBest.as<uint32_t>() + b->chainWordOff[i];
         d.cur = kUnsetCut;
@@ -640,8 +649,6 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
     CU(cudaMemcpyAsync(b->dChains.p, hc.data(), C * sizeof(DevChain), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dPhaseP.p, hp.data(), hp.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dPhaseIters.p, hi.data(), hi.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(b->dBetaEnd.p, bt.end.data(), bt.end.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(b->dBetaVal.p, bt.val.data(), bt.val.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dBits.p, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dBest.p, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     for (BatchClass& k : b->cls) {
@@ -679,6 +686,8 @@ static int rfmf_batch_run_graph_impl(rfmf_batch* b, uint64_t sweeps, int launche
     CU(cudaSetDevice(b->ctx->device));
     if (!b->graphExec || b->graphSweeps != sweeps || b->graphLaunches != launches) {
         if (b->graphExec) { cudaGraphExecDestroy(b->graphExec); b->graphExec = nullptr; }
+        // Items are sized before the capture (the graph replays them as they are).
+        if (int rc = rebalance(b)) return rc;
         cudaGraph_t graph = nullptr;
         CU(cudaStreamBeginCapture(b->ctx->stream, cudaStreamCaptureModeThreadLocal));
         int rc = RFMF_OK;
@@ -739,10 +748,11 @@ static int rfmf_batch_synchronize_impl(rfmf_batch* b) {
         if (ctl[1] != kDevOk) {
             static const char* names[] = {"ok", "carried cut value disagrees with the spins",
                                           "beta table shorter than the window", "bad work item",
-                                          "CSR bulk copy did not complete"};
+                                          "CSR bulk copy did not complete (do not reuse this context)",
+                                          "device CSR failed its check"};
             const int code = ctl[1];
             return fail(RFMF_ERR_DEVICE, "device error %d (%s) on chain %d", code,
-                        (code >= 0 && code < 5) ? names[code] : "?", ctl[2]);
+                        (code >= 0 && code < 6) ? names[code] : "?", ctl[2]);
         }
     }
     return RFMF_OK;

@@ -84,6 +84,7 @@ enum DevError : int32_t {
     kDevBetaTable = 2,       // beta table shorter than the window
     kDevBadItem = 3,         // graph/schedule index out of range
     kDevCopyTimeout = 4,     // bulk copy of the CSR did not complete in time
+    kDevBadInput = 5,        // a caller's device CSR failed the on-device check
 };
 
 // Launch-wide parameters.

@@ -190,31 +190,81 @@ int cached_runs(rfmf_context* ctx, double t0, int64_t total, std::shared_ptr<con
 
 }  // namespace
 
-int build_beta_cached(rfmf_context* ctx, const double* t0s, int64_t C, int64_t total, BetaTables& bt) {
+namespace {
+
+// The device copy of one (t0, sweeps) table, uploaded from the host table
+// `host` when no batch or request of the context holds it.
+int device_table(rfmf_context* ctx, double t0, int64_t total, const BetaRun& host, DevBetaRef& out) {
+    uint64_t bits;
+    std::memcpy(&bits, &t0, sizeof bits);
+    const auto key = std::make_pair(bits, static_cast<uint64_t>(total));
+    std::lock_guard<std::mutex> lk(ctx->devBetaMu);
+    auto it = ctx->devBeta.find(key);
+    if (it != ctx->devBeta.end()) {
+        if (DevBetaRef live = it->second.lock()) {
+            out = live;
+            return RFMF_OK;
+        }
+    }
+    auto t = std::make_shared<DevBetaTable>();
+    t->runs = static_cast<int64_t>(host.end.size());
+    if (int rc = t->end.alloc(host.end.size() * sizeof(int64_t))) return rc;
+    if (int rc = t->val.alloc(host.val.size() * sizeof(int32_t))) return rc;
+    if (!ctx->uploadStream) CU(cudaStreamCreateWithFlags(&ctx->uploadStream, cudaStreamNonBlocking));
+    CU(cudaMemcpyAsync(t->end.p, host.end.data(), host.end.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+                       ctx->uploadStream));
+    CU(cudaMemcpyAsync(t->val.p, host.val.data(), host.val.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                       ctx->uploadStream));
+    CU(cudaStreamSynchronize(ctx->uploadStream));
+    ++ctx->devBetaUploads;
+    if (ctx->devBeta.size() > 1024) {
+        for (auto e = ctx->devBeta.begin(); e != ctx->devBeta.end();)
+            e = e->second.expired() ? ctx->devBeta.erase(e) : std::next(e);
+    }
+    ctx->devBeta[key] = t;
+    ctx->devBetaKeep.push_back(t);
+    ctx->devBetaKeepBytes += static_cast<int64_t>(t->end.bytes + t->val.bytes);
+    while (ctx->devBetaKeepBytes > kDevBetaKeepBytes && ctx->devBetaKeep.size() > 1) {
+        const DevBetaRef& old = ctx->devBetaKeep.front();
+        ctx->devBetaKeepBytes -= static_cast<int64_t>(old->end.bytes + old->val.bytes);
+        ctx->devBetaKeep.pop_front();
+    }
+    out = t;
+    return RFMF_OK;
+}
+
+}  // namespace
+
+int acquire_beta(rfmf_context* ctx, const double* t0s, int64_t C, int64_t total, ChainBeta& out) {
     if (int rc = beta_range_check(t0s, C, total)) return rc;
-    bt = BetaTables{};
-    bt.chainOff.resize(C);
-    bt.chainRuns.resize(C);
-    std::map<uint64_t, std::pair<int64_t, int64_t>> placed;   // t0 bits -> (first run, runs)
+    CU(cudaSetDevice(ctx->device));
+    out = ChainBeta{};
+    out.end.resize(C);
+    out.val.resize(C);
+    out.runs.resize(C);
+    std::map<uint64_t, size_t> placed;   // t0 bits -> index into out.refs
     for (int64_t c = 0; c < C; ++c) {
         uint64_t bits;
         std::memcpy(&bits, &t0s[c], sizeof bits);
         auto it = placed.find(bits);
         if (it == placed.end()) {
-            std::shared_ptr<const BetaRun> tb;
-            if (int rc = cached_runs(ctx, t0s[c], total, tb)) return rc;
-            const int64_t first = static_cast<int64_t>(bt.end.size());
-            if (first + static_cast<int64_t>(tb->end.size()) > kMaxBetaRuns)
+            std::shared_ptr<const BetaRun> host;
+            if (int rc = cached_runs(ctx, t0s[c], total, host)) return rc;
+            out.totalRuns += static_cast<int64_t>(host->end.size());
+            if (out.totalRuns > kMaxBetaRuns)
                 return fail(RFMF_ERR_BETA_RUNS,
                             "beta run tables exceed %lld runs (t0=%g, %lld sweeps); runs scale "
                             "with log(sweeps)/t0 * 2^20",
                             static_cast<long long>(kMaxBetaRuns), t0s[c], static_cast<long long>(total));
-            bt.end.insert(bt.end.end(), tb->end.begin(), tb->end.end());
-            bt.val.insert(bt.val.end(), tb->val.begin(), tb->val.end());
-            it = placed.emplace(bits, std::make_pair(first, static_cast<int64_t>(tb->end.size()))).first;
+            DevBetaRef dev;
+            if (int rc = device_table(ctx, t0s[c], total, *host, dev)) return rc;
+            it = placed.emplace(bits, out.refs.size()).first;
+            out.refs.push_back(std::move(dev));
         }
-        bt.chainOff[c] = it->second.first;
-        bt.chainRuns[c] = it->second.second;
+        const DevBetaTable& t = *out.refs[it->second];
+        out.end[c] = t.end.as<int64_t>();
+        out.val[c] = t.val.as<int32_t>();
+        out.runs[c] = t.runs;
     }
     return RFMF_OK;
 }
@@ -261,6 +311,12 @@ extern "C" int rfmf_context_create(int device, rfmf_context** out) {
 extern "C" int rfmf_context_destroy(rfmf_context* ctx) {
     if (!ctx) return RFMF_OK;
     cudaSetDevice(ctx->device);
+    {
+        std::lock_guard<std::mutex> lk(ctx->devBetaMu);
+        ctx->devBetaKeep.clear();
+        ctx->devBeta.clear();
+    }
+    if (ctx->uploadStream) cudaStreamDestroy(ctx->uploadStream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return RFMF_OK;
@@ -270,6 +326,29 @@ extern "C" int rfmf_context_info(const rfmf_context* ctx, int* sm_count, int* sm
     if (!ctx) return fail(RFMF_ERR_INVALID, "ctx is NULL");
     if (sm_count) *sm_count = ctx->sms;
     if (smem_optin) *smem_optin = ctx->smemOptin;
+    return RFMF_OK;
+}
+
+extern "C" int rfmf_context_stream(const rfmf_context* ctx, void** stream) {
+    if (!ctx || !stream) return fail(RFMF_ERR_INVALID, "ctx/stream is NULL");
+    *stream = static_cast<void*>(ctx->stream);
+    return RFMF_OK;
+}
+
+extern "C" int rfmf_context_beta_cache(rfmf_context* ctx, int64_t* tables, int64_t* device_bytes,
+                                       uint64_t* uploads) {
+    if (!ctx) return fail(RFMF_ERR_INVALID, "ctx is NULL");
+    std::lock_guard<std::mutex> lk(ctx->devBetaMu);
+    int64_t live = 0, bytes = 0;
+    for (const auto& e : ctx->devBeta) {
+        if (DevBetaRef t = e.second.lock()) {
+            ++live;
+            bytes += static_cast<int64_t>(t->end.bytes + t->val.bytes);
+        }
+    }
+    if (tables) *tables = live;
+    if (device_bytes) *device_bytes = bytes;
+    if (uploads) *uploads = ctx->devBetaUploads;
     return RFMF_OK;
 }
 

@@ -8,6 +8,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -72,9 +73,7 @@ int append_runs(double t0, int64_t total, std::vector<int64_t>& end, std::vector
 // Refuses t0s whose beta_fixed would overflow int32 within `total` sweeps.
 int beta_range_check(const double* t0s, int64_t C, int64_t total);
 constexpr int64_t kBetaCacheRuns = int64_t(1) << 24;
-// build_beta with each distinct t0's table taken from (or added to) the
-// context's cache; thread-safe.
-int build_beta_cached(rfmf_context* ctx, const double* t0s, int64_t C, int64_t total, BetaTables& bt);
+constexpr int64_t kDevBetaKeepBytes = int64_t(256) << 20;
 bool score_safe_int32(int64_t total, double t0, int64_t B);
 
 // Launch-shape helpers of the planner.
@@ -116,6 +115,35 @@ struct DevBuf {
     }
     template <class T> T* as() const { return static_cast<T*>(p); }
 };
+
+// One (t0, sweeps) beta run table in device memory, shared by every batch,
+// drop-in call and served request of a context that anneals at that t0 over
+// that many sweeps (the reference builds and uploads one set per launch,
+// src/host_common.cpp:277-294).  Freed when its last user and the context's
+// keep-alive list let go of it.
+struct DevBetaTable {
+    DevBuf end, val;
+    int64_t runs = 0;
+};
+using DevBetaRef = std::shared_ptr<const DevBetaTable>;
+
+// Per-chain view of a set of device tables: chain c reads runs
+// [0, runs[c]) of end[c] / val[c]; refs holds one table per distinct t0.
+struct ChainBeta {
+    std::vector<const int64_t*> end;
+    std::vector<const int32_t*> val;
+    std::vector<int64_t> runs;
+    std::vector<DevBetaRef> refs;
+    int64_t totalRuns = 0;   // runs over the distinct t0s (as the reference counts them)
+};
+
+// The device tables of C chains: taken from the context when another user
+// holds (or recently held) them, else built on the host (from the host-side
+// cache) and uploaded once on the context's upload stream, which is
+// synchronised before returning, so a launch on any stream may use them.
+// Thread-safe.  RFMF_ERR_BETA_RUNS past kMaxBetaRuns runs over the distinct
+// t0s, as buildBetaRunTables refuses them.
+int acquire_beta(rfmf_context* ctx, const double* t0s, int64_t C, int64_t total, ChainBeta& out);
 
 // Request server admission.  A request's own device state: its spin and
 // best-spin words, beta run tables (8 + 4 bytes a run), schedule (4 + 8 bytes
@@ -205,6 +233,16 @@ struct rfmf_context {
     std::mutex betaMu;
     std::map<std::pair<uint64_t, uint64_t>, std::shared_ptr<const rfmf::BetaRun>> betaCache;
     int64_t betaCachedRuns = 0;
+    // Device copies of run tables by (t0 bits, sweeps): live while any batch
+    // or request holds them; the most recently acquired stay alive up to
+    // kDevBetaKeepBytes in the keep-alive list.  Uploads go through their own
+    // stream so that they never wait behind a long launch.
+    std::mutex devBetaMu;
+    std::map<std::pair<uint64_t, uint64_t>, std::weak_ptr<const rfmf::DevBetaTable>> devBeta;
+    std::deque<rfmf::DevBetaRef> devBetaKeep;
+    int64_t devBetaKeepBytes = 0;
+    uint64_t devBetaUploads = 0;
+    cudaStream_t uploadStream = nullptr;
 };
 
 // A graph in device memory: offsets and 8-byte entries for HBM walks, plus

@@ -33,7 +33,7 @@
 #include <limits>
 #include <memory>
 #include <new>
-#include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include "rfmf_host.h"
@@ -43,53 +43,120 @@ using namespace rfmf;
 // ======================================================================
 // Gset / MQLib text parser (host)
 // ======================================================================
+// The text format and the weight rule this parser implements (the loader
+// behaviour of src/read_gset.cpp:61-170, restated):
+//   * lines end at '\n'; a line that is empty after leading spaces, tabs and
+//     CRs, or whose first such character is '#', carries no data;
+//   * the first data line holds N and M (integers >= 0), the next M data
+//     lines one edge each: two integer ids and a real weight, any further
+//     text on the line ignored;
+//   * weights that are all integral (w == floor(w), |w| < 2^53) are used
+//     as they are.  Otherwise every weight is multiplied by one power of
+//     ten s = 10^k, k in 12..-12, the largest for which A s + D / 2 stays
+//     within a budget and W s within (2^31 - 1) / 2, where W is the largest
+//     |w|, and over the ids of the edge lines, A the largest sum of |w| of
+//     an id's lines and D the largest number of line ends at one id.  The
+//     budget is (2^31 - 1) / 4, or (2^63 - 1) / 8 when no k meets the first;
+//     no k at all, or W s < 1/2 (every weight would round to zero), is an
+//     error.  Scaled weights are rounded to the nearest integer, halves away
+//     from zero;
+//   * edges whose integer weight is 0 are dropped and counted; the others
+//     are returned in file order, duplicates included.
+// A forced scale s > 0 replaces the choice and its two checks.
 namespace {
 
-struct LineReader {
-    const char* p;
-    const char* end;
-    // Next data line as [b, e): blank lines and '#' comment lines skipped
-    // (first character other than space, tab or CR decides).
-    bool next(const char*& b, const char*& e) {
-        while (p < end) {
-            const char* ls = p;
-            const char* le = static_cast<const char*>(std::memchr(p, '\n', end - p));
-            if (!le) le = end;
-            p = (le < end) ? le + 1 : end;
-            const char* q = ls;
-            while (q < le && (*q == ' ' || *q == '\t' || *q == '\r')) ++q;
-            if (q == le || *q == '#') continue;
-            b = ls;
-            e = le;
-            return true;
-        }
-        return false;
+// Data lines of the text as [begin, end) spans, in order.
+std::vector<std::pair<const char*, const char*>> data_lines(const char* text, size_t len) {
+    std::vector<std::pair<const char*, const char*>> out;
+    const char* const stop = text + len;
+    for (const char* cur = text; cur < stop;) {
+        const char* nl = static_cast<const char*>(std::memchr(cur, '\n', static_cast<size_t>(stop - cur)));
+        const char* lineEnd = nl ? nl : stop;
+        const char* first = cur;
+        while (first < lineEnd && (*first == ' ' || *first == '\t' || *first == '\r')) ++first;
+        if (first < lineEnd && *first != '#') out.emplace_back(cur, lineEnd);
+        cur = nl ? nl + 1 : stop;
     }
-};
-
-// strtoll / strtod over a line that is not NUL-terminated: copy it into a
-// small buffer first (lines are short).
-struct LineBuf {
-    std::vector<char> buf;
-    const char* set(const char* b, const char* e) {
-        buf.assign(b, e);
-        buf.push_back('\0');
-        return buf.data();
-    }
-};
-
-bool integral_value(double w) {
-    return std::floor(w) == w && std::fabs(w) < 9007199254740992.0;
+    return out;
 }
 
-// Largest 10^k (k in [-12, 12]) with maxAbsB * s + maxDeg / 2 <= budgetB and
-// maxAbsW * s <= INT32_MAX / 2; 0 if none (src/read_gset.cpp:36-46).
-double choose_scale(double maxAbsB, double maxAbsW, double maxDeg, double budgetB) {
-    const double budgetW = static_cast<double>(std::numeric_limits<int32_t>::max()) / 2;
-    for (int k = 12; k >= -12; --k) {
-        const double s = std::pow(10.0, k);
-        if (maxAbsB * s + maxDeg / 2 <= budgetB && maxAbsW * s <= budgetW) return s;
+// Reads numbers off one line (a NUL-terminated copy, so the C library
+// conversions stop at its end).
+class LineScanner {
+public:
+    LineScanner(const char* b, const char* e) : text_(b, e) { text_.push_back('\0'); at_ = text_.data(); }
+    bool integer(long long& x) {
+        char* after = nullptr;
+        x = std::strtoll(at_, &after, 10);
+        return advance(after);
     }
+    bool real(double& x) {
+        char* after = nullptr;
+        x = std::strtod(at_, &after);
+        return advance(after);
+    }
+
+private:
+    bool advance(char* after) {
+        if (after == at_) return false;
+        at_ = after;
+        return true;
+    }
+    std::vector<char> text_;
+    const char* at_;
+};
+
+struct EdgeLine {
+    int64_t a, b;
+    double w;
+};
+
+bool whole_number(double w) { return w == std::floor(w) && std::fabs(w) < 9007199254740992.0; }
+
+// W, A and D of the weight rule over the edge lines.  Each line contributes
+// (id, |w|) for both of its ends; a stable sort by id keeps every id's
+// contributions in file order, so each per-id sum is accumulated in line
+// order.
+struct WeightBounds {
+    double maxAbs = 0.0, maxIdSum = 0.0, maxIdEnds = 0.0;
+};
+
+WeightBounds weight_bounds(const std::vector<EdgeLine>& lines) {
+    WeightBounds wb;
+    std::vector<std::pair<int64_t, double>> ends;
+    ends.reserve(2 * lines.size());
+    for (const EdgeLine& l : lines) {
+        const double mag = std::fabs(l.w);
+        wb.maxAbs = std::max(wb.maxAbs, mag);
+        ends.emplace_back(l.a, mag);
+        ends.emplace_back(l.b, mag);
+    }
+    std::stable_sort(ends.begin(), ends.end(),
+                     [](const std::pair<int64_t, double>& x, const std::pair<int64_t, double>& y) {
+                         return x.first < y.first;
+                     });
+    for (size_t lo = 0; lo < ends.size();) {
+        size_t hi = lo;
+        double sum = 0.0;
+        for (; hi < ends.size() && ends[hi].first == ends[lo].first; ++hi) sum += ends[hi].second;
+        wb.maxIdSum = std::max(wb.maxIdSum, sum);
+        wb.maxIdEnds = std::max(wb.maxIdEnds, static_cast<double>(hi - lo));
+        lo = hi;
+    }
+    return wb;
+}
+
+// The power of ten of the weight rule, or 0 when none qualifies.
+double power_of_ten_scale(const WeightBounds& wb) {
+    static const double kPow10[25] = {1e12, 1e11, 1e10, 1e9,  1e8,   1e7,   1e6,   1e5,  1e4,
+                                      1e3,  1e2,  1e1,  1e0,  1e-1,  1e-2,  1e-3,  1e-4, 1e-5,
+                                      1e-6, 1e-7, 1e-8, 1e-9, 1e-10, 1e-11, 1e-12};
+    const double weightCap = static_cast<double>(std::numeric_limits<int32_t>::max()) / 2;
+    const double sumCaps[2] = {static_cast<double>(std::numeric_limits<int32_t>::max()) / 4,
+                               static_cast<double>(std::numeric_limits<int64_t>::max()) / 8};
+    for (double cap : sumCaps)
+        for (double s : kPow10)
+            if (wb.maxIdSum * s + wb.maxIdEnds / 2 <= cap && wb.maxAbs * s <= weightCap) return s;
     return 0.0;
 }
 
@@ -97,18 +164,12 @@ double choose_scale(double maxAbsB, double maxAbsW, double maxDeg, double budget
 
 extern "C" int rfmf_gset_header(const char* text, size_t len, int64_t* n, int64_t* m) {
     if (!text || !n || !m) return fail(RFMF_ERR_INVALID, "text/n/m is NULL");
-    LineReader lr{text, text + len};
-    const char *b, *e;
-    if (!lr.next(b, e)) return fail(RFMF_ERR_INVALID, "no header line (numVertices numEdges)");
-    LineBuf lb;
-    const char* s = lb.set(b, e);
-    char* q = nullptr;
-    errno = 0;
-    const long long N = std::strtoll(s, &q, 10);
-    if (q == s) return fail(RFMF_ERR_INVALID, "failed to read header (numVertices numEdges)");
-    const char* s2 = q;
-    const long long M = std::strtoll(s2, &q, 10);
-    if (q == s2 || N < 0 || M < 0) return fail(RFMF_ERR_INVALID, "failed to read header (numVertices numEdges)");
+    const auto lines = data_lines(text, len);
+    long long N = -1, M = -1;
+    if (lines.empty()) return fail(RFMF_ERR_INVALID, "no data line: the first must hold the vertex and edge counts");
+    LineScanner sc(lines[0].first, lines[0].second);
+    if (!sc.integer(N) || !sc.integer(M) || N < 0 || M < 0)
+        return fail(RFMF_ERR_INVALID, "the first data line must hold two counts >= 0 (vertices, edges)");
     *n = N;
     *m = M;
     return RFMF_OK;
@@ -121,90 +182,48 @@ static int rfmf_gset_parse_impl(const char* text, size_t len, double forced_scal
     int64_t N = 0, M = 0;
     if (int rc = rfmf_gset_header(text, len, &N, &M)) return rc;
     if (cap < M) return fail(RFMF_ERR_CAPACITY, "cap %lld < %lld edges", (long long)cap, (long long)M);
-    LineReader lr{text, text + len};
-    const char *b, *e;
-    lr.next(b, e);   // header
-    std::vector<double> ew(static_cast<size_t>(M));
-    LineBuf lb;
-    bool floatWeights = false;
+    const auto lines = data_lines(text, len);
+    if (static_cast<int64_t>(lines.size()) - 1 < M)
+        return fail(RFMF_ERR_INVALID, "header announces %lld edges, the text has %lld edge lines",
+                    (long long)M, (long long)(lines.size() - 1));
+    std::vector<EdgeLine> edges(static_cast<size_t>(M));
+    bool allWhole = true;
     for (int64_t i = 0; i < M; ++i) {
-        if (!lr.next(b, e)) return fail(RFMF_ERR_INVALID, "failed to read edge %lld", (long long)i);
-        const char* p = lb.set(b, e);
-        char* q = nullptr;
-        const long long a = std::strtoll(p, &q, 10);
-        if (q == p) return fail(RFMF_ERR_INVALID, "bad edge line %lld", (long long)i);
-        p = q;
-        const long long c = std::strtoll(p, &q, 10);
-        if (q == p) return fail(RFMF_ERR_INVALID, "bad edge line %lld", (long long)i);
-        p = q;
-        const double x = std::strtod(p, &q);
-        if (q == p) return fail(RFMF_ERR_INVALID, "bad edge line %lld", (long long)i);
-        if (!integral_value(x)) floatWeights = true;
-        u[i] = a;
-        v[i] = c;
-        ew[i] = x;
+        LineScanner sc(lines[i + 1].first, lines[i + 1].second);
+        long long a = 0, b = 0;
+        double x = 0.0;
+        if (!sc.integer(a) || !sc.integer(b) || !sc.real(x))
+            return fail(RFMF_ERR_INVALID, "edge line %lld: expected two ids and a weight", (long long)i);
+        edges[i] = EdgeLine{a, b, x};
+        allWhole = allWhole && whole_number(x);
     }
-    // Per-vertex bounds of the raw edges for the scale choice.
-    double maxAbsB = 0.0, maxAbsW = 0.0, maxDeg = 0.0;
-    {
-        bool dense = true;
-        for (int64_t i = 0; i < M && dense; ++i)
-            dense = u[i] >= 0 && u[i] <= N && v[i] >= 0 && v[i] <= N;
-        if (dense) {
-            std::vector<double> absB(static_cast<size_t>(N + 1), 0.0);
-            std::vector<int64_t> deg(static_cast<size_t>(N + 1), 0);
-            for (int64_t i = 0; i < M; ++i) {
-                const double aw = std::fabs(ew[i]);
-                maxAbsW = std::max(maxAbsW, aw);
-                absB[u[i]] += aw;
-                absB[v[i]] += aw;
-                ++deg[u[i]];
-                ++deg[v[i]];
-            }
-            for (double x : absB) maxAbsB = std::max(maxAbsB, x);
-            for (int64_t d : deg) maxDeg = std::max(maxDeg, static_cast<double>(d));
-        } else {
-            std::unordered_map<int64_t, double> absB;
-            std::unordered_map<int64_t, int64_t> deg;
-            for (int64_t i = 0; i < M; ++i) {
-                const double aw = std::fabs(ew[i]);
-                maxAbsW = std::max(maxAbsW, aw);
-                absB[u[i]] += aw;
-                absB[v[i]] += aw;
-                ++deg[u[i]];
-                ++deg[v[i]];
-            }
-            for (const auto& kv : absB) maxAbsB = std::max(maxAbsB, kv.second);
-            for (const auto& kv : deg) maxDeg = std::max(maxDeg, static_cast<double>(kv.second));
-        }
-    }
-    double scale = 1.0;
+    double s = 1.0;
     if (forced_scale > 0.0) {
-        scale = forced_scale;
-    } else if (floatWeights) {
-        scale = choose_scale(maxAbsB, maxAbsW, maxDeg, static_cast<double>(std::numeric_limits<int32_t>::max()) / 4);
-        if (scale == 0.0)
-            scale = choose_scale(maxAbsB, maxAbsW, maxDeg, static_cast<double>(std::numeric_limits<int64_t>::max()) / 8);
-        if (scale == 0.0)
-            return fail(RFMF_ERR_INVALID, "no power-of-10 scale fits these weights (max|w|=%g, maxB=%g)",
-                        maxAbsW, maxAbsB);
-        if (maxAbsW * scale < 0.5)
-            return fail(RFMF_ERR_INVALID, "chosen scale %g rounds every weight to 0", scale);
+        s = forced_scale;
+    } else if (!allWhole) {
+        const WeightBounds wb = weight_bounds(edges);
+        s = power_of_ten_scale(wb);
+        if (s == 0.0)
+            return fail(RFMF_ERR_INVALID, "weights too large for any power-of-ten scale (max |w| %g, max id |w| sum %g)",
+                        wb.maxAbs, wb.maxIdSum);
+        if (wb.maxAbs * s < 0.5)
+            return fail(RFMF_ERR_INVALID, "at scale %g every weight rounds to zero (max |w| %g)", s, wb.maxAbs);
     }
-    // Round, drop zeros, keep file order (no dedup here).
-    int64_t k = 0, dropped = 0;
-    for (int64_t i = 0; i < M; ++i) {
-        const int64_t wi = (scale == 1.0 && integral_value(ew[i])) ? static_cast<int64_t>(ew[i])
-                                                                   : std::llround(ew[i] * scale);
-        if (wi == 0) { ++dropped; continue; }
-        u[k] = u[i];
-        v[k] = v[i];
-        w[k] = wi;
-        ++k;
+    int64_t kept = 0, zeros = 0;
+    for (const EdgeLine& l : edges) {
+        const int64_t iw = (s == 1.0 && whole_number(l.w)) ? static_cast<int64_t>(l.w) : std::llround(l.w * s);
+        if (iw == 0) {
+            ++zeros;
+            continue;
+        }
+        u[kept] = l.a;
+        v[kept] = l.b;
+        w[kept] = iw;
+        ++kept;
     }
-    *nedges = k;
-    if (scale_out) *scale_out = scale;
-    if (zero_dropped) *zero_dropped = dropped;
+    *nedges = kept;
+    if (scale_out) *scale_out = s;
+    if (zero_dropped) *zero_dropped = zeros;
     return RFMF_OK;
 }
 

@@ -8,22 +8,34 @@
 // synchronises the device and can fail at the worst moment), and embedders
 // that hand the library pre-sized buffers only.  Such a caller passes its
 // inputs and outputs as device buffers; everything else the kernel needs
-// (chain records, work items, the work-queue head and the error word) lives
-// in g_noallocScratch below, which every GPU that loads this library holds
-// until the process exits.
+// (graph and schedule records, chain records, work items, the work-queue head
+// and the error word) lives in g_noallocScratch below, a fixed 476,672-byte
+// array that every GPU that loads this library holds until the process exits.
 //
 // Set-up: the first call on a device, with that device current, looks up
 // the array's device address (cudaGetSymbolAddress) and caches it; make that
 // first call before any stream capture.  The array is shared by every call
 // and keeps the last call's contents; each call rewrites the records and
-// clears the queue head and error word before its launch.  Calls whose
+// clears the queue head and error word before its launches.  Calls whose
 // launches overlap on the GPU (different streams, or different host threads
 // on one device) race on the array: serialise them.
+//
+// The caller's CSR is checked on the device before the anneal (the host
+// never sees it): offsets start at 0 and never decrease, every neighbour id
+// is in range and not the row itself, rows are strictly ascending, every
+// entry has a twin of equal weight, and no row's sum of |w| exceeds the
+// caller's max_weighted_deg (which picks the gain width and the score path,
+// so an understated bound would overflow them).  A CSR that fails sets the
+// error word and moves the work-queue head past every work item, so the
+// anneal launch that follows takes no work; the call then returns
+// RFMF_ERR_INVALID.  The only host synchronisation is the read of the error
+// word at the end of the call.
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <cstddef>
 #include <cmath>
+#include <cstddef>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <limits>
@@ -36,6 +48,7 @@
 
 namespace rfmf {
 int set_last_error(int code, const char* msg);
+int fail(int code, const char* fmt, ...);
 const void* kernel_ptr(int dbytes, int fmt, bool s64);
 cudaError_t launch_anneal(const DevLaunch& L, int dbytes, int fmt, bool s64, int grid,
                           int threads, size_t smem, cudaStream_t stream);
@@ -62,7 +75,7 @@ constexpr size_t kOffOrder = (kOffItems + kNoAllocMaxChains * sizeof(DevItem) + 
 constexpr size_t kNoAllocScratchBytes =
     (kOffOrder + kNoAllocMaxChains * sizeof(int32_t) + 255) & ~size_t(255);
 static_assert(sizeof(DevGraph) <= 256 && sizeof(DevSchedule) <= 256, "record slots too small");
-static_assert(kNoAllocScratchBytes <= 640 * 1024, "no-alloc scratch larger than stated");
+static_assert(kNoAllocScratchBytes == 476672, "the no-alloc scratch size is stated in rfmf.h");
 
 // The scratch itself: file-scope, statically sized, one per device.
 static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
@@ -88,29 +101,54 @@ int scratch_address(int device, unsigned char** out) {
     return RFMF_OK;
 }
 
-}  // namespace
+// Records a failed check: the first code wins, and the queue head moves past
+// any work-item count so the anneal launch that follows takes no work.
+__device__ __forceinline__ void reject(int32_t* ctl) {
+    atomicCAS(ctl + 1, 0, static_cast<int32_t>(kDevBadInput));
+    atomicExch(ctl, 1 << 30);
+}
 
-namespace {
-
-// One-block reduction of the weight column of the 8-byte entries into *out
-// (the sum of weights over directed entries), used by the set-up below.
-__global__ void wsum_kernel(const int32_t* edges, int64_t m2, int64_t* out) {
-    __shared__ long long part[32];
-    long long acc = 0;
-    for (int64_t i = threadIdx.x; i < m2; i += blockDim.x) acc += edges[2 * i + 1];
-    for (int m = 16; m > 0; m >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, m);
-    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        long long t = 0;
-        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) t += part[w];
-        *out = t;
+// Checks the caller's CSR (one thread per row, grid-stride; every read stays
+// inside [0, offsets[n]) once the row bounds are checked) and adds the sum of
+// the weights over directed entries into the graph record's wsum2, which the
+// kernel uses to derive each fresh chain's cut.
+__global__ void check_csr_kernel(const uint32_t* __restrict__ off, const int2* __restrict__ edges,
+                                 int n, long long maxB, long long* wsum2, int32_t* ctl) {
+    const uint32_t m2 = off[n];
+    if (blockIdx.x == 0 && threadIdx.x == 0 && off[0] != 0) reject(ctl);
+    long long wsum = 0;
+    bool bad = false;
+    const int stride = gridDim.x * blockDim.x;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n && !bad; v += stride) {
+        const uint32_t lo = off[v], hi = off[v + 1];
+        if (hi < lo || hi > m2) { bad = true; break; }
+        long long absSum = 0;
+        int prev = -1;
+        for (uint32_t i = lo; i < hi; ++i) {
+            const int2 e = edges[i];
+            if (e.x < 0 || e.x >= n || e.x == v || e.x <= prev) { bad = true; break; }
+            prev = e.x;
+            absSum += (e.y < 0) ? -static_cast<long long>(e.y) : static_cast<long long>(e.y);
+            wsum += e.y;
+            // The twin (e.x, v) with the same weight, by bisection of row e.x.
+            const uint32_t rowEnd = off[e.x + 1];
+            uint32_t a = off[e.x], b = rowEnd;
+            if (b < a || b > m2) { bad = true; break; }
+            while (a < b) {
+                const uint32_t mid = a + (b - a) / 2;
+                if (edges[mid].x < v) a = mid + 1; else b = mid;
+            }
+            if (a >= rowEnd || edges[a].x != v || edges[a].y != e.y) { bad = true; break; }
+        }
+        if (absSum > maxB) bad = true;
     }
+    if (bad) reject(ctl);
+    for (int m = 16; m > 0; m >>= 1) wsum += __shfl_xor_sync(0xFFFFFFFFu, wsum, m);
+    if ((threadIdx.x & 31) == 0 && wsum != 0)
+        atomicAdd(reinterpret_cast<unsigned long long*>(wsum2), static_cast<unsigned long long>(wsum));
 }
-cudaError_t noalloc_wsum(const int32_t* edges, int64_t m2, int64_t* out, cudaStream_t stream) {
-    wsum_kernel<<<1, 1024, 0, stream>>>(edges, m2, out);
-    return cudaGetLastError();
-}
+
+bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
 
 }  // namespace
 
@@ -120,9 +158,9 @@ static int rfmf_anneal_noalloc_impl(int device, void* stream, int64_t n,
                                    const uint64_t* solver_seeds, int64_t nphases,
                                    const uint64_t* phases, const uint64_t* iters,
                                    const int64_t* d_beta_end, const int32_t* d_beta_val,
-                                   const int64_t* chain_beta_off, const int64_t* chain_beta_runs,
-                                   uint32_t* d_spin_bits, uint32_t* d_best_bits,
-                                   int64_t* d_cur, int64_t* d_best) {
+                                   int64_t beta_runs, const int64_t* chain_beta_off,
+                                   const int64_t* chain_beta_runs, uint32_t* d_spin_bits,
+                                   uint32_t* d_best_bits, int64_t* d_cur, int64_t* d_best) {
     if (n <= 0 || n >= (int64_t(1) << 31)) return nerr(RFMF_ERR_INVALID, "n out of range");
     if (C <= 0 || C > kNoAllocMaxChains)
         return nerr(RFMF_ERR_CAPACITY, "no-alloc path: chains must be 1..4096");
@@ -132,8 +170,26 @@ static int rfmf_anneal_noalloc_impl(int device, void* stream, int64_t n,
         !chain_beta_off || !chain_beta_runs || !d_spin_bits || !d_best_bits || !d_cur || !d_best ||
         (nphases && (!phases || !iters)))
         return nerr(RFMF_ERR_INVALID, "NULL argument");
+    // The kernel reads offsets and spin words as 4-byte words, CSR entries as
+    // 8-byte {col, weight} pairs and beta run ends and cut values as 8-byte
+    // words: a pointer off those boundaries is refused here, before any
+    // device work.
+    if (!aligned(d_offsets, 4) || !aligned(d_edges, 8) || !aligned(d_beta_end, 8) ||
+        !aligned(d_beta_val, 4) || !aligned(d_spin_bits, 4) || !aligned(d_best_bits, 4) ||
+        !aligned(d_cur, 8) || !aligned(d_best, 8))
+        return nerr(RFMF_ERR_INVALID,
+                    "misaligned device pointer (offsets, beta_val, spin and best bits need 4 "
+                    "bytes; edges, beta_end and the cut outputs 8)");
     if (max_weighted_deg < 0 || max_weighted_deg > std::numeric_limits<int32_t>::max())
         return nerr(RFMF_ERR_INVALID, "max_weighted_deg out of range");
+    if (beta_runs < 1) return nerr(RFMF_ERR_INVALID, "beta_runs must be >= 1");
+    for (int64_t c = 0; c < C; ++c) {
+        if (chain_beta_off[c] < 0 || chain_beta_runs[c] < 1 ||
+            chain_beta_runs[c] > beta_runs - chain_beta_off[c])
+            return rfmf::fail(RFMF_ERR_INVALID, "chain %lld: beta runs outside the %lld-run table",
+                              static_cast<long long>(c), static_cast<long long>(beta_runs));
+        if (!(t0s[c] > 0.0)) return nerr(RFMF_ERR_INVALID, "t0 must be > 0");
+    }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (cudaSetDevice(device) != cudaSuccess) return nerr(RFMF_ERR_CUDA, "cudaSetDevice failed");
     unsigned char* base = nullptr;
@@ -144,8 +200,6 @@ static int rfmf_anneal_noalloc_impl(int device, void* stream, int64_t n,
         if (phases[p] > 0x7FFFFFFFull) return nerr(RFMF_ERR_CAPACITY, "phase P too large");
         if (phases[p]) { total += iters[p]; maxP = std::max<uint64_t>(maxP, phases[p]); }
     }
-    for (int64_t c = 0; c < C; ++c)
-        if (!(t0s[c] > 0.0)) return nerr(RFMF_ERR_INVALID, "t0 must be > 0");
 
     // Launch plan: CSR walked in HBM (the caller's buffers), one warp per
     // chain, int8 gains when B <= 127, compact int32 keys when the range
@@ -165,9 +219,9 @@ static int rfmf_anneal_noalloc_impl(int device, void* stream, int64_t n,
     const int words = static_cast<int>((n + 31) / 32);
     const int pmax = static_cast<int>(std::min<uint64_t>(maxP, static_cast<uint64_t>(n)));
     const uint32_t chainBytes = chain_layout(static_cast<int>(n), words, pmax, W, dbytes).total;
-    int dev = device, sms = 0, optin = 0;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    int sms = 0, optin = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess)
         return nerr(RFMF_ERR_CUDA, "device attribute query failed");
     const void* kern = kernel_ptr(dbytes, kCsrGlobal, s64);
     cudaFuncAttributes fa{};
@@ -197,18 +251,17 @@ static int rfmf_anneal_noalloc_impl(int device, void* stream, int64_t n,
     const size_t smem = kSmemHeader + static_cast<size_t>(K) * chainBytes;
 
     // Records into the scratch array (plain copies; nothing is allocated on
-    // the device; the host staging below is ordinary host memory).
+    // the device; the host staging below is ordinary host memory).  wsum2
+    // starts at 0 and the check kernel adds the weights into it.
     DevGraph g{};
     g.offsets = d_offsets;
     g.edges = reinterpret_cast<const Edge*>(d_edges);
     g.compact = nullptr;
     g.n = static_cast<int32_t>(n);
     g.words = words;
+    g.wsum2 = 0;
     g.offBytes = 0;
     g.entBytes = 0;
-    // wsum2 (sum of weights over directed entries) is not known without the
-    // host CSR: chains start fresh, so the kernel's cut check is not used and
-    // the cut is derived from D and wsum2 -- compute wsum2 on the device.
     DevSchedule sch{reinterpret_cast<const uint32_t*>(base + kOffPhaseP),
                     reinterpret_cast<const uint64_t*>(base + kOffPhaseIters),
                     static_cast<int32_t>(nphases), 0};
@@ -239,27 +292,28 @@ static int rfmf_anneal_noalloc_impl(int device, void* stream, int64_t n,
         items[i] = DevItem{0, static_cast<int32_t>(i * K),
                            static_cast<int32_t>(std::min<int64_t>(K, C - static_cast<int64_t>(i) * K)), 0};
 
-    // wsum2 on the device: the sum of the weight column, reduced by a
-    // one-block kernel into the graph record (no temporary buffers).
     cudaError_t e = cudaSuccess;
     auto cp = [&](size_t off, const void* src, size_t bytes) {
         if (e == cudaSuccess) e = cudaMemcpyAsync(base + off, src, bytes, cudaMemcpyHostToDevice, st);
     };
+    cp(kOffGraph, &g, sizeof g);
     cp(kOffSched, &sch, sizeof sch);
     cp(kOffPhaseP, hp.data(), hp.size() * sizeof(uint32_t));
     cp(kOffPhaseIters, hi.data(), hi.size() * sizeof(uint64_t));
     cp(kOffChains, ch.data(), C * sizeof(DevChain));
     cp(kOffItems, items.data(), nitems * sizeof(DevItem));
     cp(kOffOrder, order.data(), C * sizeof(int32_t));
-    cp(kOffGraph, &g, sizeof g);
-    // m2 from the device offsets array (one 4-byte read).
-    uint32_t m2 = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&m2, d_offsets + n, sizeof m2, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e == cudaSuccess)
-        e = noalloc_wsum(d_edges, m2, reinterpret_cast<int64_t*>(base + kOffGraph +
-                                                                        offsetof(DevGraph, wsum2)), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(base + kOffCtl, 0, 16, st);
+    int32_t* ctl = reinterpret_cast<int32_t*>(base + kOffCtl);
+    if (e == cudaSuccess) {
+        const int threads = 256;
+        const int blocks = static_cast<int>(std::min<int64_t>((n + threads - 1) / threads, 8 * static_cast<int64_t>(sms)));
+        check_csr_kernel<<<blocks, threads, 0, st>>>(
+            d_offsets, reinterpret_cast<const int2*>(d_edges), static_cast<int>(n),
+            static_cast<long long>(max_weighted_deg),
+            reinterpret_cast<long long*>(base + kOffGraph + offsetof(DevGraph, wsum2)), ctl);
+        e = cudaGetLastError();
+    }
     if (e != cudaSuccess) return nerr(RFMF_ERR_CUDA, cudaGetErrorString(e));
 
     DevLaunch L{};
@@ -278,9 +332,9 @@ static int rfmf_anneal_noalloc_impl(int device, void* stream, int64_t n,
     L.pmax = pmax;
     L.csrBytes = 0;
     L.chainBytes = chainBytes;
-    L.queue = reinterpret_cast<int32_t*>(base + kOffCtl);
-    L.error = reinterpret_cast<int32_t*>(base + kOffCtl) + 1;
-    L.errorItem = reinterpret_cast<int32_t*>(base + kOffCtl) + 2;
+    L.queue = ctl;
+    L.error = ctl + 1;
+    L.errorItem = ctl + 2;
     L.itemNs = nullptr;
     L.window = total;
     for (int i = 0; i < 16; ++i)
@@ -294,11 +348,16 @@ static int rfmf_anneal_noalloc_impl(int device, void* stream, int64_t n,
     if (e == cudaSuccess)
         e = cudaMemcpy2DAsync(d_best, sizeof(int64_t), base + kOffChains + offsetof(DevChain, best),
                               sizeof(DevChain), sizeof(int64_t), C, cudaMemcpyDeviceToDevice, st);
-    int32_t ctl[4] = {0, 0, 0, 0};
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ctl, base + kOffCtl, sizeof ctl, cudaMemcpyDeviceToHost, st);
+    int32_t hctl[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hctl, ctl, sizeof hctl, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return nerr(RFMF_ERR_CUDA, cudaGetErrorString(e));
-    if (ctl[1] != kDevOk) return nerr(RFMF_ERR_DEVICE, "device-side error during the anneal");
+    if (hctl[1] == kDevBadInput)
+        return nerr(RFMF_ERR_INVALID,
+                    "device CSR rejected: offsets must start at 0 and never decrease, ids lie in "
+                    "[0, n) without self loops, rows strictly ascending, every entry has a twin of "
+                    "equal weight, and no row's sum of |w| may exceed max_weighted_deg");
+    if (hctl[1] != kDevOk) return nerr(RFMF_ERR_DEVICE, "device-side error during the anneal");
     return RFMF_OK;
 }
 
@@ -309,14 +368,14 @@ extern "C" int rfmf_anneal_noalloc(int device, void* stream, int64_t n,
                                    const uint64_t* solver_seeds, int64_t nphases,
                                    const uint64_t* phases, const uint64_t* iters,
                                    const int64_t* d_beta_end, const int32_t* d_beta_val,
-                                   const int64_t* chain_beta_off, const int64_t* chain_beta_runs,
-                                   uint32_t* d_spin_bits, uint32_t* d_best_bits,
-                                   int64_t* d_cur, int64_t* d_best) {
+                                   int64_t beta_runs, const int64_t* chain_beta_off,
+                                   const int64_t* chain_beta_runs, uint32_t* d_spin_bits,
+                                   uint32_t* d_best_bits, int64_t* d_cur, int64_t* d_best) {
     try {
         return rfmf_anneal_noalloc_impl(device, stream, n, d_offsets, d_edges, max_weighted_deg, C,
                                         t0s, solver_seeds, nphases, phases, iters, d_beta_end,
-                                        d_beta_val, chain_beta_off, chain_beta_runs, d_spin_bits,
-                                        d_best_bits, d_cur, d_best);
+                                        d_beta_val, beta_runs, chain_beta_off, chain_beta_runs,
+                                        d_spin_bits, d_best_bits, d_cur, d_best);
     } catch (const std::bad_alloc&) {
         return rfmf::set_last_error(RFMF_ERR_NOMEM, "host allocation failed in rfmf_anneal_noalloc");
     } catch (...) {

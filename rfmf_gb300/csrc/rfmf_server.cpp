@@ -47,13 +47,13 @@ struct Request {
     uint64_t total = 0;
     int pmax = 1;
     std::vector<uint32_t> initBits;   // C * words
-    BetaTables bt;                    // host run tables until admission
+    ChainBeta beta;                   // the context's shared device beta tables
     // launch class
     int dbytes = 1, fmt = kCsrGlobal, W = 1;
     bool s64 = false;
     int64_t devBytes = 0;             // request_device_bytes: counted against max_device_bytes
     // device state (worker thread only)
-    DevBuf dBits, dBest, dBetaEnd, dBetaVal, dPhaseP, dPhaseIters;
+    DevBuf dBits, dBest, dPhaseP, dPhaseIters;
     int64_t slot0 = -1;               // first of C consecutive chain slots
     int graphSlot = -1, schedSlot = -1;
     uint64_t done = 0;                // sweeps completed by every chain
@@ -211,16 +211,11 @@ int admit(rfmf_server* s, Request& r) {
     const int64_t CW = r.C * r.words;
     int rc;
     if ((rc = r.dBits.alloc(CW * 4)) || (rc = r.dBest.alloc(CW * 4))) return rc;
-    const BetaTables& bt = r.bt;
-    if ((rc = r.dBetaEnd.alloc(bt.end.size() * 8)) || (rc = r.dBetaVal.alloc(bt.val.size() * 4)))
-        return rc;
     const size_t np = std::max<size_t>(r.phaseP.size(), 1);
     if ((rc = r.dPhaseP.alloc(np * 4)) || (rc = r.dPhaseIters.alloc(np * 8))) return rc;
     cudaStream_t st = s->stream;
     CU(cudaMemcpyAsync(r.dBits.p, r.initBits.data(), CW * 4, cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(r.dBest.p, r.initBits.data(), CW * 4, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(r.dBetaEnd.p, bt.end.data(), bt.end.size() * 8, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(r.dBetaVal.p, bt.val.data(), bt.val.size() * 4, cudaMemcpyHostToDevice, st));
     if (!r.phaseP.empty()) {
         CU(cudaMemcpyAsync(r.dPhaseP.p, r.phaseP.data(), r.phaseP.size() * 4, cudaMemcpyHostToDevice, st));
         CU(cudaMemcpyAsync(r.dPhaseIters.p, r.phaseIters.data(), r.phaseIters.size() * 8,
@@ -283,9 +278,9 @@ int admit(rfmf_server* s, Request& r) {
         d.graph = r.graphSlot;
         d.sched = r.schedSlot;
         d.solverSeed = r.seeds[c];
-        d.betaEnd = r.dBetaEnd.as<int64_t>() + bt.chainOff[c];
-        d.betaVal = r.dBetaVal.as<int32_t>() + bt.chainOff[c];
-        d.betaRuns = bt.chainRuns[c];
+        d.betaEnd = r.beta.end[c];
+        d.betaVal = r.beta.val[c];
+        d.betaRuns = r.beta.runs[c];
         d.spinBits = r.dBits.as<uint32_t>() + c * r.words;
         d.bestBits = r.dBest.as<uint32_t>() + c * r.words;
         d.cur = kUnsetCut;
@@ -299,7 +294,6 @@ int admit(rfmf_server* s, Request& r) {
     CU(cudaStreamSynchronize(st));
     r.initBits.clear();
     r.initBits.shrink_to_fit();
-    r.bt = BetaTables{};
     return RFMF_OK;
 }
 
@@ -317,7 +311,8 @@ void release(rfmf_server* s, Request& r) {
     }
     if (r.schedSlot >= 0) s->freeSchedSlots.push_back(r.schedSlot);
     r.schedSlot = -1;
-    for (DevBuf* b : {&r.dBits, &r.dBest, &r.dBetaEnd, &r.dBetaVal, &r.dPhaseP, &r.dPhaseIters}) {
+    r.beta = ChainBeta{};   // drops this request's holds on the shared beta tables
+    for (DevBuf* b : {&r.dBits, &r.dBest, &r.dPhaseP, &r.dPhaseIters}) {
         if (b->p) cudaFree(b->p);
         b->p = nullptr;
         b->bytes = 0;
@@ -689,12 +684,15 @@ static int rfmf_submit_impl(rfmf_server* s, const rfmf_graph* g, int64_t nchains
         if (!(t0s[c] > 0.0)) return fail(RFMF_ERR_INVALID, "t0s[%lld] must be > 0", static_cast<long long>(c));
     r->total = total;
     r->pmax = static_cast<int>(std::max<uint64_t>(1, std::min<uint64_t>(maxP, static_cast<uint64_t>(g->n))));
-    // Run tables on the submitting thread (from the context's cache when
-    // another batch or request used the same t0 and length), never on the
-    // worker, where building them would stall the launch windows.
-    if (int rc = build_beta_cached(s->ctx, r->t0s.data(), nchains, static_cast<int64_t>(total), r->bt))
+    // Run tables on the submitting thread, never on the worker, where
+    // building or uploading them would stall the launch windows: the
+    // context's device copies when another batch or request holds the same
+    // (t0, sweeps), else built (from the host cache) and uploaded once.
+    if (int rc = acquire_beta(s->ctx, r->t0s.data(), nchains, static_cast<int64_t>(total), r->beta))
         return rc;
-    r->devBytes = request_device_bytes(nchains, r->words, static_cast<int64_t>(r->bt.end.size()),
+    // The admission footprint counts the request's beta tables in full even
+    // when it shares them with other users.
+    r->devBytes = request_device_bytes(nchains, r->words, r->beta.totalRuns,
                                        static_cast<int64_t>(r->phaseP.size()));
     if (s->maxDeviceBytes && r->devBytes > s->maxDeviceBytes)
         return fail(RFMF_ERR_CAPACITY, "request needs %lld device bytes, above max_device_bytes %lld",

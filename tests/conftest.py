@@ -71,6 +71,16 @@ def ref_host():
     return L
 
 
+@pytest.fixture(scope="session")
+def refgpu():
+    """The reference's own kernel (oracle/_ref/anneal_kernels.cubin, built from
+    its sources by oracle/build_ref.sh) launched through oracle/refgpu.py."""
+    import refgpu as RG
+    if not RG.available():
+        pytest.skip("reference kernel cubin not built on this machine")
+    return RG
+
+
 def chains_for(g, seeds):
     """Initial spins (from raw seeds) and solver seeds, as setupSolver/main do."""
     import oracle as ora

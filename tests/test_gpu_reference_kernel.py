@@ -4,19 +4,9 @@ oracle/build_ref.sh) is present: same inputs, bit-identical outputs."""
 import numpy as np
 import pytest
 
-from conftest import ROOT, chains_for
+from conftest import chains_for
 
 pytestmark = pytest.mark.gpu
-
-
-@pytest.fixture(scope="module")
-def refgpu():
-    import sys
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import refgpu as RG
-    if not RG.available():
-        pytest.skip("reference kernel cubin not built on this machine")
-    return RG
 
 
 @pytest.mark.parametrize("shape", ["er", "torus", "tree", "int64"])

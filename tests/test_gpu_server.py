@@ -164,3 +164,53 @@ def test_server_device_byte_budget(rfmf, ctx):
         srv.submit(dg, two["init"], two["t0s"], two["phases"], two["iters"], two["solver"])
     assert ei.value.code == 4
     srv.close()
+
+
+def test_device_beta_tables_shared_within_a_context(rfmf, ctx):
+    """Beta run tables live on the device once per (t0, sweeps) per context:
+    a second batch, an rfmf_anneal call and a served request on the same
+    ladder and length upload nothing more, while a new length uploads its
+    own tables; every result still equals a standalone anneal (on another
+    context, with its own tables)."""
+    c = rfmf.Context(0)
+    g = rfmf.erdos_renyi(400, 0.04, signed=True, seed=18)
+    dg = rfmf.DeviceGraph(c, g)
+    dref = rfmf.DeviceGraph(ctx, g)
+    ladder = [35.0, 50.0, 70.0, 100.0, 140.0, 200.0, 280.0, 400.0]
+    phases, iters = [32, 4, 1], [300, 300, 300]
+    assert c.beta_cache()["uploads"] == 0
+    r1 = _request(rfmf, g, list(range(900, 916)), ladder * 2, phases, iters)
+    b1 = rfmf.Batch(c, [dg] * 16, r1["t0s"], r1["solver"], list(r1["init"]), phases, iters)
+    assert c.beta_cache()["uploads"] == 8 and c.beta_cache()["tables"] == 8
+    r2 = _request(rfmf, g, list(range(950, 966)), ladder * 2, phases, iters)
+    b2 = rfmf.Batch(c, [dg] * 16, r2["t0s"], r2["solver"], list(r2["init"]), phases, iters)
+    got = rfmf.anneal_gpu(c, dg, g.max_weighted_degree(), r1["init"], r1["t0s"], phases, iters,
+                          r1["solver"])
+    srv = rfmf.Server(c, window_sweeps=250)
+    rid = srv.submit(dg, r2["init"], r2["t0s"], phases, iters, r2["solver"])
+    assert srv.wait(rid, timeout=300)["state"] == "done"
+    served = srv.result(rid)
+    srv.close()
+    assert c.beta_cache()["uploads"] == 8
+    for b in (b1, b2):
+        b.run(sum(iters))
+    o1, o2 = b1.read(), b2.read()
+    b1.close()
+    b2.close()
+    ref1 = _standalone(rfmf, ctx, dref, r1)
+    ref2 = _standalone(rfmf, ctx, dref, r2)
+    _same(got, ref1)
+    _same(served, ref2)
+    assert np.array_equal(np.stack(o1["best_spins"]), ref1.best_spins)
+    assert np.array_equal(o1["best_vals"], ref1.best_vals)
+    assert np.array_equal(np.stack(o2["end_spins"]), ref2.end_spins)
+    assert np.array_equal(o2["cur_vals"], ref2.final_vals)
+    # another length: its own tables
+    got3 = rfmf.anneal_gpu(c, dg, g.max_weighted_degree(), r1["init"], r1["t0s"], phases,
+                           [100, 100, 100], r1["solver"])
+    assert c.beta_cache()["uploads"] == 16
+    _same(got3, rfmf.anneal_gpu(ctx, dref, g.max_weighted_degree(), r1["init"], r1["t0s"], phases,
+                                [100, 100, 100], r1["solver"]))
+    dg.close()
+    dref.close()
+    c.close()
