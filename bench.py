@@ -291,6 +291,20 @@ def gpu_arm(args, rank, world):
     cfg = R.make_config(threads_per_chain=args.threads, chains_per_cta=args.chains_per_cta)
     base = rank * args.chains
     setup = chain_setup(graphs, args.chains, base)
+    tuned = None
+    if not args.no_autotune:
+        # measured plan: candidates timed on a compressed copy of the schedule
+        gl_, ini_, sol_, t0_ = [], [], [], []
+        for k, s_ in enumerate(setup):
+            gl_ += [dgs[k]] * len(s_["seeds"])
+            ini_ += list(s_["init"])
+            sol_ += s_["solver"]
+            t0_ += s_["t0s"]
+        cfg, cands = R.autotune(ctx, gl_, t0_, sol_, ini_, phases, iters, base=cfg)
+        tuned = {"chosen": {"threads_per_chain": cfg.threads_per_chain, "csr_format": cfg.csr_format},
+                 "candidates": [{"threads_per_chain": c.threads_per_chain, "csr_format": c.csr_format,
+                                 "us_per_chain_sweep": round(us, 5)} for c, us in cands],
+                 "note": "0 = the planner's rule; csr_format 3 = HBM walks"}
 
     def batch_for(setup_, ph, it):
         gl, ini, sol, t0 = [], [], [], []
@@ -434,12 +448,15 @@ def gpu_arm(args, rank, world):
             "chains_per_cta": info["chains_per_cta"],
             "grid": info["grid"],
             "csr": {1: "unit16 in shared memory", 2: "packed32 in shared memory",
-                    3: "HBM"}[info["csr_format"]],
+                    3: "HBM, 8-byte entries", 4: "HBM, 16-bit entries",
+                    5: "HBM, 32-bit entries"}[info["csr_format"]],
             "gain_bytes": info["gain_width"],
             "items": info["items"],
             "balanced_items": bool(info["balanced"]),
             "score_path": "int64" if info["score64"] else "int32",
             "launch_classes": info.get("launch_classes"),
+            "plan": "rfmf_autotune (measured)" if tuned else "planner rules",
+            "autotune": tuned,
             "l2": "flushed (256 MB write) between timed steps",
             "parallelism": f"replicas x{world}",
         },
@@ -967,6 +984,8 @@ def main():
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--chains-per-cta", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="plan the batch with the planner's rules instead of measuring candidates")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--plain-sweeps", type=int, default=16000)
     ap.add_argument("--no-cpu", action="store_true")

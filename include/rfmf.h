@@ -179,7 +179,9 @@ typedef struct rfmf_launch_config {
     int threads_per_chain; /* 0 = auto, else 32, 64, 128 or 256 (one chain's warp group) */
     int score_path;        /* 0 = gate (src/host_common.cpp:296-312), 1 = int32, 2 = int64 */
     int chains_per_cta;    /* 0 = auto, else chains sharing one CTA's copy of the graph */
-    int csr_format;        /* 0 = auto, 1 = unit16 (shared), 2 = packed32 (shared), 3 = HBM */
+    int csr_format;        /* 0 = auto, 1 = unit16 (shared), 2 = packed32 (shared),
+                              3 = HBM (the graph's most compact entries: 2, 4 or 8 bytes),
+                              4 = HBM with 8-byte {col, weight} entries */
     int gain_width;        /* 0 = auto, 1 = int8 (needs B <= 127), 4 = int32 */
 } rfmf_launch_config;
 
@@ -245,6 +247,49 @@ int rfmf_batch_synchronize(rfmf_batch* b);
 int rfmf_batch_read(rfmf_batch* b, int8_t* end_spins, int8_t* best_spins,
                     int64_t* cur_vals, int64_t* best_vals, uint64_t* sweeps_done);
 
+/*
+ * Resume from saved state (no reference counterpart: a chain is a pure
+ * function of its graph, seed, t0, schedule and sweep index,
+ * src/anneal_gpu.cuh:4-8, so what rfmf_batch_read returns is a checkpoint).
+ * Creates a batch like rfmf_batch_create whose chain c starts from
+ * end_spins / best_spins (concatenated like initial_spins), cur_vals[c] /
+ * best_vals[c] (their cut values) and sweeps_done[c] <= the schedule's total;
+ * running it to the end of the schedule gives exactly the results of one
+ * uninterrupted run.  The cut values are recomputed from the spins on the
+ * device and a checkpoint whose values disagree is refused
+ * (RFMF_ERR_INVALID).  The improved-sweeps statistic restarts at 0.
+ */
+int rfmf_batch_restore(rfmf_context* ctx, int64_t nchains, const rfmf_graph* const* graphs,
+                       const double* t0s, const uint64_t* solver_seeds, int64_t nphases,
+                       const uint64_t* phases, const uint64_t* iters,
+                       const rfmf_launch_config* cfg, const int8_t* end_spins,
+                       const int8_t* best_spins, const int64_t* cur_vals,
+                       const int64_t* best_vals, const uint64_t* sweeps_done, rfmf_batch** out);
+
+/*
+ * Measured launch planning (in place of the reference's fixed V100 table,
+ * src/tuning.hpp:10-17, applied at src/anneal_kernels.cu:641-662).  Times
+ * candidate plans on short trial batches of these very chains (their graphs,
+ * seeds, t0s and initial spins; the schedule compressed to trial_sweeps
+ * sweeps with every phase keeping its share, 0 = 512) and writes the fastest
+ * to *best, starting from *base (NULL: all automatic).  Candidates: warps per
+ * chain from the planner's rule or fixed at 1, 2 or 4, each with the rule's
+ * CSR residency or with HBM walks.  Each candidate runs twice and keeps its
+ * faster time.  Results never depend on the plan.  The choice is cached in
+ * the context under the batch's shape (graph sizes, chains per graph,
+ * schedule), so later calls for the same shape return at once.  If cand_us
+ * is not NULL it receives each candidate's microseconds per chain-sweep (at
+ * most *ncand entries; *ncand is set to the candidate count, and a candidate
+ * that cannot be planned gets a negative time), and cand (may be NULL) the
+ * candidates' configs.
+ */
+int rfmf_autotune(rfmf_context* ctx, int64_t nchains, const rfmf_graph* const* graphs,
+                  const double* t0s, const uint64_t* solver_seeds, const int8_t* initial_spins,
+                  int64_t nphases, const uint64_t* phases, const uint64_t* iters,
+                  uint64_t trial_sweeps, const rfmf_launch_config* base,
+                  rfmf_launch_config* best, int* ncand, rfmf_launch_config* cand,
+                  float* cand_us);
+
 /* The launch plan the autotuner chose for a batch. */
 typedef struct rfmf_batch_plan {
     int64_t nchains;
@@ -254,7 +299,8 @@ typedef struct rfmf_batch_plan {
     int grid;                  /* persistent CTAs per launch */
     int items;                 /* work items (chain groups) per launch */
     int score64;               /* 1 if the int64 score path is used */
-    int csr_format;            /* 1 unit16, 2 packed32, 3 HBM */
+    int csr_format;            /* 1 unit16, 2 packed32 (shared memory); HBM walks of
+                                  3 8-byte, 4 16-bit, 5 32-bit entries */
     int gain_width;            /* bytes per vertex gain: 1 or 4 */
     int smem_bytes;            /* dynamic shared memory per CTA */
     int balanced;              /* 1 once every multi-graph launch class sizes its work items from learned graph costs */
@@ -302,7 +348,8 @@ enum rfmf_request_state {
     RFMF_REQ_QUEUED = 0,
     RFMF_REQ_RUNNING = 1,
     RFMF_REQ_DONE = 2,
-    RFMF_REQ_FAILED = 3
+    RFMF_REQ_FAILED = 3,
+    RFMF_REQ_CANCELLED = 4
 };
 
 typedef struct rfmf_request_status {
@@ -346,6 +393,15 @@ int rfmf_result(rfmf_server* s, uint64_t request_id, int8_t* end_spins, int8_t* 
                 int64_t* best_vals, int64_t* final_vals);
 
 int rfmf_server_stats_get(rfmf_server* s, rfmf_server_stats* out);
+
+/* Cancel a request (no reference counterpart: the reference runs one solve
+ * per process and stops only by exiting).  A queued request is cancelled at
+ * once; a running one leaves at the next window boundary, its device state
+ * and chain slots freed for the requests behind it (the others' results are
+ * unaffected).  Its state becomes RFMF_REQ_CANCELLED; rfmf_wait returns for
+ * it and rfmf_result releases it with RFMF_ERR_INVALID.  Cancelling a request
+ * that has already finished changes nothing. */
+int rfmf_cancel(rfmf_server* s, uint64_t request_id);
 
 /*
  * The annealer for callers that cannot allocate device memory.  No reference

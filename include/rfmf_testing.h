@@ -20,6 +20,15 @@ extern "C" {
  * besides exit). */
 int rfmf_batch_debug_set_cut(rfmf_batch* b, int64_t chain, int64_t cut);
 
+/* Injected host allocation failure: the `countdown`-th host allocation
+ * checkpoint reached from now on (Gset parsing, batch creation and restore,
+ * request submission, admission and result read-out in a server's worker,
+ * batch read-out) fails as if
+ * the host were out of memory, and the calls above it report RFMF_ERR_NOMEM
+ * (a served request fails; the server and the context stay usable).
+ * countdown <= 0 disarms it.  Process-wide. */
+int rfmf_debug_fail_host_alloc(int64_t countdown);
+
 #ifdef __cplusplus
 }
 #endif

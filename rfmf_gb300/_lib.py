@@ -46,7 +46,12 @@ SIGNATURES = [
     ("rfmf_batch_debug_set_cut", ct.c_int, [_P, _I64, _I64]),
     ("rfmf_batch_synchronize", ct.c_int, [_P]),
     ("rfmf_batch_read", ct.c_int, [_P, _P, _P, _P, _P, _P]),
+    ("rfmf_batch_restore", ct.c_int, [_P, _I64, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P,
+                                      _P, _P]),
+    ("rfmf_debug_fail_host_alloc", ct.c_int, [_I64]),
     ("rfmf_batch_info", ct.c_int, [_P, _P]),
+    ("rfmf_autotune", ct.c_int, [_P, _I64, _P, _P, _P, _P, _I64, _P, _P, _U64, _P, _P, _P, _P,
+                                 _P]),
     ("rfmf_batch_destroy", ct.c_int, [_P]),
     ("rfmf_anneal_noalloc", ct.c_int, [ct.c_int, _P, _I64, _P, _P, _I64, _I64, _P, _P, _I64,
                                        _P, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _P]),
@@ -65,6 +70,7 @@ SIGNATURES = [
     ("rfmf_wait", ct.c_int, [_P, _U64, ct.c_double, _P]),
     ("rfmf_result", ct.c_int, [_P, _U64, _P, _P, _P, _P]),
     ("rfmf_server_stats_get", ct.c_int, [_P, _P]),
+    ("rfmf_cancel", ct.c_int, [_P, _U64]),
 ]
 
 
@@ -106,7 +112,7 @@ class ServerStats(ct.Structure):
                 ("done", ct.c_int64)]
 
 
-REQUEST_STATES = {0: "queued", 1: "running", 2: "done", 3: "failed"}
+REQUEST_STATES = {0: "queued", 1: "running", 2: "done", 3: "failed", 4: "cancelled"}
 
 STATUS = {0: "RFMF_OK", 1: "RFMF_ERR_INVALID", 2: "RFMF_ERR_CUDA", 3: "RFMF_ERR_NOMEM",
           4: "RFMF_ERR_CAPACITY", 5: "RFMF_ERR_DEVICE", 6: "RFMF_ERR_BETA_RUNS"}

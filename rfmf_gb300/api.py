@@ -102,7 +102,8 @@ def beta_tables(t0s, total):
 def make_config(threads_per_chain=0, score_path=0, chains_per_cta=0, csr_format=0,
                 gain_width=0, corr=0, s_width=32, device=0):
     """rfmf_launch_config; 0 everywhere = autotuned.  csr_format: 1 unit16,
-    2 packed32, 3 HBM; gain_width: 1 (int8) or 4 (int32)."""
+    2 packed32 (shared memory), 3 HBM (most compact entries), 4 HBM 8-byte
+    entries; gain_width: 1 (int8) or 4 (int32)."""
     c = LaunchConfig()
     c.corr = corr
     c.device = device
@@ -252,8 +253,64 @@ def anneal_gpu(ctx, dgraph, max_weighted_deg, initial_spins_, t0s, phases, iters
     return AnnealResult(end, best, ms.value, bv, fv)
 
 
+def autotune(ctx, dgraphs, t0s, solver_seeds, init_spins, phases, iters, trial_sweeps=0,
+             base=None):
+    """rfmf_autotune: time candidate launch plans on short trial batches of
+    these chains; returns (best config, [(candidate config, us per
+    chain-sweep), ...]).  Cached in the context by batch shape."""
+    C = len(dgraphs)
+    garr = (ct.c_void_p * C)(*[g.h.value for g in dgraphs])
+    t = np.ascontiguousarray(t0s, np.float64)
+    sd = np.array([int(s) % 2**64 for s in solver_seeds], np.uint64)
+    flat = np.ascontiguousarray(np.concatenate([np.asarray(s, np.int8) for s in init_spins]))
+    ph = np.ascontiguousarray(phases, np.uint64)
+    it = np.ascontiguousarray(iters, np.uint64)
+    best = LaunchConfig()
+    n = ct.c_int(16)
+    cands = (LaunchConfig * 16)()
+    us = np.zeros(16, np.float32)
+    check(lib().rfmf_autotune(ctx.h, C, garr, _p(t), _p(sd), _p(flat), len(ph), _p(ph), _p(it),
+                              int(trial_sweeps), ct.byref(base) if base is not None else None,
+                              ct.byref(best), ct.byref(n), cands, _p(us)))
+    return best, [(cands[k], float(us[k])) for k in range(min(n.value, 16))]
+
+
+def debug_fail_host_alloc(countdown):
+    """Testing aid: the countdown-th host allocation checkpoint from now on
+    fails as if out of memory (rfmf_debug_fail_host_alloc); 0 disarms."""
+    check(lib().rfmf_debug_fail_host_alloc(int(countdown)))
+
+
 class Batch:
     """Chains over many graphs with device-resident state (rfmf_batch)."""
+
+    @classmethod
+    def restore(cls, ctx, dgraphs, t0s, solver_seeds, phases, iters, state, cfg=None):
+        """A batch resumed from saved state: `state` is what read() returned
+        (end_spins, best_spins, cur_vals, best_vals, sweeps_done)."""
+        self = cls.__new__(cls)
+        C = len(dgraphs)
+        self.C = C
+        self.ns = [g.n for g in dgraphs]
+        self.ctx = ctx
+        self.dgraphs = list(dgraphs)
+        garr = (ct.c_void_p * C)(*[g.h.value for g in dgraphs])
+        t = np.ascontiguousarray(t0s, np.float64)
+        sd = np.array([int(s) % 2**64 for s in solver_seeds], np.uint64)
+        end = np.ascontiguousarray(np.concatenate([np.asarray(x, np.int8) for x in state["end_spins"]]))
+        best = np.ascontiguousarray(np.concatenate([np.asarray(x, np.int8) for x in state["best_spins"]]))
+        cur = np.ascontiguousarray(state["cur_vals"], np.int64)
+        bv = np.ascontiguousarray(state["best_vals"], np.int64)
+        done = np.ascontiguousarray(state["sweeps_done"], np.uint64)
+        ph = np.ascontiguousarray(phases, np.uint64)
+        it = np.ascontiguousarray(iters, np.uint64)
+        cfg = cfg or make_config()
+        h = ct.c_void_p()
+        check(lib().rfmf_batch_restore(ctx.h, C, garr, _p(t), _p(sd), len(ph), _p(ph), _p(it),
+                                       ct.byref(cfg), _p(end), _p(best), _p(cur), _p(bv), _p(done),
+                                       ct.byref(h)))
+        self.h = h
+        return self
 
     def __init__(self, ctx, dgraphs, t0s, solver_seeds, init_spins, phases, iters, cfg=None):
         C = len(dgraphs)
@@ -401,13 +458,17 @@ class Server:
         best = np.zeros((C, n), np.int8)
         bv = np.zeros(C, np.int64)
         fv = np.zeros(C, np.int64)
-        finished = self.poll(rid)["state"] in ("done", "failed")
+        finished = self.poll(rid)["state"] in ("done", "failed", "cancelled")
         try:
             check(lib().rfmf_result(self.h, int(rid), _p(end), _p(best), _p(bv), _p(fv)))
         finally:
             if finished:
                 self._req.pop(rid, None)
         return AnnealResult(end, best, 0.0, bv, fv)
+
+    def cancel(self, rid):
+        """Cancel a queued or running request (rfmf_cancel)."""
+        check(lib().rfmf_cancel(self.h, int(rid)))
 
     def stats(self):
         s = ServerStats()

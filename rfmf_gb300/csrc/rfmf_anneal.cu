@@ -18,7 +18,8 @@
 //     D[v] = spin[v]*S[v] (the per-vertex gain; int8 with a +128 bias when
 //     the max weighted degree B <= 127, else int32), the spins as bits, and
 //     the best-so-far spins as bits.  Graphs too big for shared memory walk
-//     their CSR in HBM instead (kCsrGlobal); the chain state stays resident.
+//     their CSR in HBM instead, in the most compact entry form they allow
+//     (2, 4 or 8 bytes); the chain state stays resident.
 //   * SELECT reads only D.  The sweep-uniform part of the Philox counter is
 //     hoisted (rounds 1-3 lose 3 multiplies and 3 xors per block) and three
 //     vertex blocks are in flight per thread.
@@ -284,6 +285,9 @@ struct Csr<kCsrUnit16> {
         lo = c.off[v];
         hi = c.off[v + 1];
     }
+    __device__ static __forceinline__ uint32_t raw(const CsrView& c, uint32_t i) {
+        return static_cast<const uint16_t*>(c.ent)[i];
+    }
     __device__ static __forceinline__ void entry(const CsrView& c, uint32_t i, int& col, int& w) {
         const uint32_t e = static_cast<const uint16_t*>(c.ent)[i];
         col = static_cast<int>(e >> 1);
@@ -314,6 +318,37 @@ struct Csr<kCsrGlobal> {
         const int2 e = __ldg(static_cast<const int2*>(c.ent) + i);
         col = e.x;
         w = e.y;
+    }
+};
+
+// The compact entries read from HBM on the read-only path: a quarter (16-bit)
+// or half (32-bit) of the bytes of the {col, w} pairs per entry.
+template <>
+struct Csr<kCsrGlobal16> {
+    __device__ static __forceinline__ void row(const CsrView& c, int v, uint32_t& lo, uint32_t& hi) {
+        lo = __ldg(c.off + v);
+        hi = __ldg(c.off + v + 1);
+    }
+    __device__ static __forceinline__ uint32_t raw(const CsrView& c, uint32_t i) {
+        return __ldg(static_cast<const unsigned short*>(c.ent) + i);
+    }
+    __device__ static __forceinline__ void entry(const CsrView& c, uint32_t i, int& col, int& w) {
+        const uint32_t e = raw(c, i);
+        col = static_cast<int>(e >> 1);
+        w = 1 - 2 * static_cast<int>(e & 1u);
+    }
+};
+
+template <>
+struct Csr<kCsrGlobal32> {
+    __device__ static __forceinline__ void row(const CsrView& c, int v, uint32_t& lo, uint32_t& hi) {
+        lo = __ldg(c.off + v);
+        hi = __ldg(c.off + v + 1);
+    }
+    __device__ static __forceinline__ void entry(const CsrView& c, uint32_t i, int& col, int& w) {
+        const uint32_t e = __ldg(static_cast<const unsigned int*>(c.ent) + i);
+        col = static_cast<int>(e & 0xFFFFu);
+        w = static_cast<int32_t>(e) >> 16;
     }
 };
 
@@ -550,20 +585,20 @@ __device__ __forceinline__ void flip_winner(const ChainSmem& s, int g, int v, Lo
 // lane col & 3 of word col >> 2 (the biased bytes never carry, see D8).
 // (At smaller P the generic walk, which spreads a row over several lanes,
 // is faster.)
+template <int kFmt>
 __device__ __forceinline__ void flip2_unit16_d8_warp(const ChainSmem& s, const CsrView& csr, int P, int lane) {
-    const uint16_t* ent = static_cast<const uint16_t*>(csr.ent);
     unsigned int* Dw = reinterpret_cast<unsigned int*>(s.D);
     const unsigned char* sb = s.sb;
     for (int gi = lane; gi < P; gi += 32) {
         const int v = s.win[gi];
         if (v < 0) continue;
         const uint32_t sv = sb[v];
-        uint32_t i = csr.off[v];
-        const uint32_t hi = csr.off[v + 1];
+        uint32_t i, hi;
+        Csr<kFmt>::row(csr, v, i, hi);
         for (; i + 4 <= hi; i += 4) {
             uint32_t e[4], sx[4];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) e[j] = ent[i + j];
+            for (int j = 0; j < 4; ++j) e[j] = Csr<kFmt>::raw(csr, i + j);
 #pragma unroll
             for (int j = 0; j < 4; ++j) sx[j] = sb[e[j] >> 1];
 #pragma unroll
@@ -573,7 +608,7 @@ __device__ __forceinline__ void flip2_unit16_d8_warp(const ChainSmem& s, const C
             }
         }
         for (; i < hi; ++i) {
-            const uint32_t e0 = ent[i];
+            const uint32_t e0 = Csr<kFmt>::raw(csr, i);
             const uint32_t neg = (sv ^ sb[e0 >> 1] ^ e0) & 1u;
             atomicAdd(Dw + (e0 >> 3), (neg ? 0xFFFFFFFEu : 2u) << ((e0 & 6u) << 2));
         }
@@ -995,9 +1030,14 @@ __device__ void run_chain(const DevLaunch& L, const ChainSmem& s, const CsrView&
 
         // ---- FLIP 2: D[x] += 2 w s_b s_x over the winners' rows (new spins);
         // `lanes` consecutive threads share a row, four entries in flight.
-        if (kFmt == kCsrUnit16 && std::is_same<DP, D8>::value && T == 32 && P >= 64) {
-            flip2_unit16_d8_warp(s, csr, P, t);
-        } else {
+        bool walked = false;
+        if constexpr ((kFmt == kCsrUnit16 || kFmt == kCsrGlobal16) && std::is_same<DP, D8>::value) {
+            if (T == 32 && P >= 64) {
+                flip2_unit16_d8_warp<kFmt>(s, csr, P, t);
+                walked = true;
+            }
+        }
+        if (!walked) {
             const int lanes = 1 << pc.laneShift;
             const int sub = t & (lanes - 1);
             for (int gi = t >> pc.laneShift; gi < P; gi += T >> pc.laneShift) {
@@ -1140,7 +1180,7 @@ __global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) 
     const ChainSmem cs = carve_chain(chainBase + static_cast<size_t>(grp) * L.chainBytes, L, kDBytes);
 
     if (threadIdx.x < 16) lut[threadIdx.x] = L.lut[threadIdx.x];
-    if (kFmt != kCsrGlobal && threadIdx.x == 0) mbar_init(mbar);
+    if (!csr_in_hbm(kFmt) && threadIdx.x == 0) mbar_init(mbar);
     __syncthreads();
 
     uint32_t phase = 0;
@@ -1160,9 +1200,9 @@ __global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) 
         if (threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
         const DevGraph& g = L.graphs[item.graph];
         CsrView csr;
-        if constexpr (kFmt == kCsrGlobal) {
+        if constexpr (csr_in_hbm(kFmt)) {
             csr.off = g.offsets;
-            csr.ent = g.edges;
+            csr.ent = (kFmt == kCsrGlobal) ? static_cast<const void*>(g.edges) : g.compact;
         } else {
             if (item.graph != loaded) {
                 // All threads agree on the outcome, so that a chain's
@@ -1204,29 +1244,22 @@ __global__ void __launch_bounds__(512, 1) rfmf_anneal_kernel(const DevLaunch L) 
 }  // namespace
 
 // ------------------------------------------------------------ host hooks
-// Kernel variants: D width {1, 4} x CSR format {unit16, packed32, global} x
-// score {int32, int64}.
+// Kernel variants: D width {1, 4} x CSR format {unit16, packed32, HBM 8-byte,
+// HBM 16-bit, HBM 32-bit} x score {int32, int64}.
+template <int DB, bool S>
+const void* kernel_for_format(int fmt) {
+    switch (fmt) {
+        case kCsrUnit16: return reinterpret_cast<const void*>(&rfmf_anneal_kernel<DB, kCsrUnit16, S>);
+        case kCsrPacked32: return reinterpret_cast<const void*>(&rfmf_anneal_kernel<DB, kCsrPacked32, S>);
+        case kCsrGlobal16: return reinterpret_cast<const void*>(&rfmf_anneal_kernel<DB, kCsrGlobal16, S>);
+        case kCsrGlobal32: return reinterpret_cast<const void*>(&rfmf_anneal_kernel<DB, kCsrGlobal32, S>);
+        default: return reinterpret_cast<const void*>(&rfmf_anneal_kernel<DB, kCsrGlobal, S>);
+    }
+}
+
 const void* kernel_ptr(int dbytes, int fmt, bool s64) {
-#define RFMF_K(DB, F, S) reinterpret_cast<const void*>(&rfmf_anneal_kernel<DB, F, S>)
-    if (dbytes == 1) {
-        if (s64) {
-            if (fmt == kCsrUnit16) return RFMF_K(1, kCsrUnit16, true);
-            if (fmt == kCsrPacked32) return RFMF_K(1, kCsrPacked32, true);
-            return RFMF_K(1, kCsrGlobal, true);
-        }
-        if (fmt == kCsrUnit16) return RFMF_K(1, kCsrUnit16, false);
-        if (fmt == kCsrPacked32) return RFMF_K(1, kCsrPacked32, false);
-        return RFMF_K(1, kCsrGlobal, false);
-    }
-    if (s64) {
-        if (fmt == kCsrUnit16) return RFMF_K(4, kCsrUnit16, true);
-        if (fmt == kCsrPacked32) return RFMF_K(4, kCsrPacked32, true);
-        return RFMF_K(4, kCsrGlobal, true);
-    }
-    if (fmt == kCsrUnit16) return RFMF_K(4, kCsrUnit16, false);
-    if (fmt == kCsrPacked32) return RFMF_K(4, kCsrPacked32, false);
-    return RFMF_K(4, kCsrGlobal, false);
-#undef RFMF_K
+    if (dbytes == 1) return s64 ? kernel_for_format<1, true>(fmt) : kernel_for_format<1, false>(fmt);
+    return s64 ? kernel_for_format<4, true>(fmt) : kernel_for_format<4, false>(fmt);
 }
 
 cudaError_t launch_anneal(const DevLaunch& L, int dbytes, int fmt, bool s64, int grid,

@@ -20,8 +20,10 @@
 #include <algorithm>
 #include <cstddef>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
+#include <string>
 #include <memory>
 #include <new>
 #include <tuple>
@@ -188,15 +190,15 @@ int plan_class(rfmf_batch& b, BatchClass& k, const rfmf_launch_config& c, bool e
 void plan_balanced(const rfmf_batch& b, BatchClass& k) {
     const size_t G = k.graphs.size();
     bool known = true;
-    for (int gi : k.graphs) known = known && b.glist[gi]->costNs > 0.0;
+    for (int gi : k.graphs) known = known && b.glist[gi]->cost(k.warps, k.fmt) > 0.0;
     if (!known || G < 2) { k.balanced = false; return; }
     const int64_t slots = static_cast<int64_t>(k.occ) * b.ctx->sms;
     double lo = 0.0, hi = 0.0;
-    for (int gi : k.graphs) hi = std::max(hi, b.glist[gi]->costNs * k.K);
+    for (int gi : k.graphs) hi = std::max(hi, b.glist[gi]->cost(k.warps, k.fmt) * k.K);
     auto fits = [&](double tau, std::vector<int>& kg) {
         int64_t items = 0;
         for (size_t q = 0; q < G; ++q) {
-            int v = static_cast<int>(std::floor(tau / b.glist[k.graphs[q]]->costNs));
+            int v = static_cast<int>(std::floor(tau / b.glist[k.graphs[q]]->cost(k.warps, k.fmt)));
             v = std::max(1, std::min(k.K, v));
             kg[q] = v;
             items += (static_cast<int64_t>(k.chainsOf[q].size()) + v - 1) / v;
@@ -222,7 +224,8 @@ void build_items(const rfmf_batch& b, BatchClass& k) {
     for (size_t q = 0; q < G; ++q) gorder[q] = static_cast<int>(q);
     auto itemCost = [&](int q) {
         const rfmf_graph* g = b.glist[k.graphs[q]];
-        const double c = g->costNs > 0.0 ? g->costNs : static_cast<double>(g->n);
+        const double learned = g->cost(k.warps, k.fmt);
+        const double c = learned > 0.0 ? learned : static_cast<double>(g->n);
         return c * k.Kg[q];
     };
     std::stable_sort(gorder.begin(), gorder.end(), [&](int a, int z) { return itemCost(a) > itemCost(z); });
@@ -266,8 +269,7 @@ int harvest_item_times(rfmf_batch& b, BatchClass& k) {
         const double w = static_cast<double>(it.count) * static_cast<double>(sweeps);
         const double c = static_cast<double>(ns[i]) / w;
         const rfmf_graph* g = b.glist[it.graph];
-        g->costNs = (g->costNs * g->costWeight + c * w) / (g->costWeight + w);
-        g->costWeight += w;
+        g->learn(k.warps, k.fmt, c, w);
     }
     return RFMF_OK;
 }
@@ -316,13 +318,25 @@ int enqueue_run(rfmf_batch* b, uint64_t sweeps, bool capturing = false) {
 
 }  // namespace
 
+// Saved chain state a batch starts from (rfmf_batch_restore).
+struct Resume {
+    const int8_t* best_spins;
+    const int64_t* cur_vals;
+    const int64_t* best_vals;
+    const uint64_t* sweeps_done;
+};
+
+// rfmf_batch_create, and with `resume` set rfmf_batch_restore (initial_spins
+// are then the saved end spins).
 static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph* const* graphs,
                                  const double* t0s, const uint64_t* solver_seeds,
                                  const int8_t* initial_spins, int64_t nphases,
                                  const uint64_t* phases, const uint64_t* iters,
-                                 const rfmf_launch_config* cfg, rfmf_batch** out) {
+                                 const rfmf_launch_config* cfg, rfmf_batch** out,
+                                 const Resume* resume = nullptr) {
     if (!ctx || !out) return fail(RFMF_ERR_INVALID, "ctx/out is NULL");
     *out = nullptr;
+    host_alloc_point();
     if (C <= 0 || C > (int64_t(1) << 30)) return fail(RFMF_ERR_INVALID, "nchains=%lld", (long long)C);
     if (!graphs || !t0s || !solver_seeds || !initial_spins)
         return fail(RFMF_ERR_INVALID, "NULL per-chain array");
@@ -335,7 +349,7 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
         return fail(RFMF_ERR_INVALID, "threads_per_chain must be 0, 32, 64, 128 or 256");
     if (c.gain_width != 0 && c.gain_width != 1 && c.gain_width != 4)
         return fail(RFMF_ERR_INVALID, "gain_width must be 0, 1 or 4");
-    if (c.csr_format < 0 || c.csr_format > 3) return fail(RFMF_ERR_INVALID, "csr_format must be 0..3");
+    if (c.csr_format < 0 || c.csr_format > 4) return fail(RFMF_ERR_INVALID, "csr_format must be 0..4");
     if (c.score_path < 0 || c.score_path > 2) return fail(RFMF_ERR_INVALID, "score_path must be 0..2");
     const int64_t totalAll = rfmf_total_steps(nphases, iters);   // src/host_common.cpp:196-210
     if (totalAll < 0) return fail(RFMF_ERR_CAPACITY, "iters total more than 10^12 sweeps");
@@ -432,10 +446,13 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
                 if (g->unit16 && fits(kCsrUnit16)) pk.fmt = kCsrUnit16;
                 else if (g->packed32 && fits(kCsrPacked32)) pk.fmt = kCsrPacked32;
             }
+            // Walked in HBM: the most compact entries the graph has, unless
+            // the 8-byte pairs are asked for.
+            if (pk.fmt == kCsrGlobal && c.csr_format != 4) pk.fmt = hbm_format(g);
             cudaFuncAttributes fa{};
             const int64_t dynMax = dyn_smem_max(ctx, kernel_ptr(dbytes, pk.fmt, pk.s64), fa);
             const int64_t room = dynMax - static_cast<int64_t>(kSmemHeader) -
-                                 (pk.fmt == kCsrGlobal ? 0 : static_cast<int64_t>(csr_bytes(g, pk.fmt)));
+                                 (csr_in_hbm(pk.fmt) ? 0 : static_cast<int64_t>(csr_bytes(g, pk.fmt)));
             const int64_t warpCap = std::min(16 / Wc, Wc > 1 ? 15 : 16);
             pk.resident = std::max<int64_t>(0, std::min<int64_t>({perSm, warpCap, room / chainB}));
             return RFMF_OK;
@@ -487,7 +504,7 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
     if (c.csr_format == 0) {
         const int64_t perSm = (b->C + ctx->sms - 1) / std::max(ctx->sms, 1);
         for (size_t ci = 0; ci < b->cls.size(); ++ci) {
-            if (b->cls[ci].fmt == kCsrGlobal) continue;
+            if (csr_in_hbm(b->cls[ci].fmt)) continue;
             cudaFuncAttributes fa{};
             const int64_t dynMax =
                 dyn_smem_max(ctx, kernel_ptr(b->cls[ci].dbytes, b->cls[ci].fmt, b->cls[ci].score64), fa);
@@ -521,14 +538,15 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
                 k.chainsOf.erase(k.chainsOf.begin() + static_cast<std::ptrdiff_t>(worst));
                 const int dbytes = k.dbytes, W = k.warps, pmax = k.pmax;
                 const bool s64 = k.score64;
-                const Key gk{dbytes, kCsrGlobal, W, s64 ? 1 : 0};
+                const int hf = hbm_format(b->glist[gi]);
+                const Key gk{dbytes, hf, W, s64 ? 1 : 0};
                 auto it = classOf.find(gk);
                 if (it == classOf.end()) {
                     it = classOf.emplace(gk, static_cast<int>(b->cls.size())).first;
                     b->cls.emplace_back();     // invalidates k
                     BatchClass& h = b->cls.back();
                     h.dbytes = dbytes;
-                    h.fmt = kCsrGlobal;
+                    h.fmt = hf;
                     h.warps = W;
                     h.score64 = s64;
                     h.pmax = pmax;
@@ -552,8 +570,10 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
     const bool exact = b->cls.size() > 1;
     for (BatchClass& k : b->cls) {
         int rc = plan_class(*b, k, c, exact);
-        if (rc == RFMF_ERR_CAPACITY && k.fmt != kCsrGlobal && c.csr_format == 0) {
-            k.fmt = kCsrGlobal;    // the class's largest CSR and largest n together do not fit
+        if (rc == RFMF_ERR_CAPACITY && !csr_in_hbm(k.fmt) && c.csr_format == 0) {
+            // The class's largest CSR and largest n together do not fit: its
+            // graphs (all of them 16-bit or all 32-bit capable) walk HBM.
+            k.fmt = (k.fmt == kCsrUnit16) ? kCsrGlobal16 : kCsrGlobal32;
             rc = plan_class(*b, k, c, exact);
         }
         if (rc) return rc;
@@ -573,7 +593,7 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
         const int fmt = b->cls[graphClass[gi]].fmt;
         hg[gi].offsets = g->offsets.as<uint32_t>();
         hg[gi].edges = g->edges.as<Edge>();
-        hg[gi].compact = (fmt == kCsrUnit16) ? g->u16.p : (fmt == kCsrPacked32 ? g->p32.p : nullptr);
+        hg[gi].compact = compact_entries(g, fmt);
         hg[gi].n = static_cast<int32_t>(g->n);
         hg[gi].words = static_cast<int32_t>((g->n + 31) / 32);
         hg[gi].wsum2 = g->wsum2;
@@ -591,12 +611,27 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
     }
     b->words = b->chainWordOff[C];
     std::vector<uint32_t> bits(static_cast<size_t>(std::max<int64_t>(b->words, 1)), 0u);
+    std::vector<uint32_t> bestBits;
     {
         size_t sp = 0;
         for (int64_t i = 0; i < C; ++i) {
             pack_spins(initial_spins + sp, b->chainN[i], bits.data() + b->chainWordOff[i]);
             sp += static_cast<size_t>(b->chainN[i]);
         }
+    }
+    if (resume) {
+        bestBits.assign(bits.size(), 0u);
+        size_t sp = 0;
+        uint64_t least = total;
+        for (int64_t i = 0; i < C; ++i) {
+            if (resume->sweeps_done[i] > total)
+                return fail(RFMF_ERR_INVALID, "chain %lld: %llu sweeps done, the schedule has %llu", (long long)i,
+                            (unsigned long long)resume->sweeps_done[i], (unsigned long long)total);
+            least = std::min<uint64_t>(least, resume->sweeps_done[i]);
+            pack_spins(resume->best_spins + sp, b->chainN[i], bestBits.data() + b->chainWordOff[i]);
+            sp += static_cast<size_t>(b->chainN[i]);
+        }
+        b->hostDone = least;
     }
 
     // Device buffers.
@@ -636,9 +671,9 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
         d.betaRuns = cb.runs[i];
         d.spinBits = b->dBits.as<uint32_t>() + b->chainWordOff[i];
         d.bestBits = b->dBest.as<uint32_t>() + b->chainWordOff[i];
-        d.cur = kUnsetCut;
-        d.best = kUnsetCut;
-        d.sweepsDone = 0;
+        d.cur = resume ? resume->cur_vals[i] : kUnsetCut;
+        d.best = resume ? resume->best_vals[i] : kUnsetCut;
+        d.sweepsDone = resume ? resume->sweeps_done[i] : 0;
         d.sweepsTotal = total;
         d.improvedSweeps = 0;
     }
@@ -650,7 +685,8 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
     CU(cudaMemcpyAsync(b->dPhaseP.p, hp.data(), hp.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dPhaseIters.p, hi.data(), hi.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(b->dBits.p, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(b->dBest.p, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(b->dBest.p, resume ? bestBits.data() : bits.data(), bits.size() * sizeof(uint32_t),
+                       cudaMemcpyHostToDevice, st));
     for (BatchClass& k : b->cls) {
         if ((rc = upload_items(*b, k))) return rc;
         CU(cudaMemsetAsync(k.dCtl.p, 0, 4 * sizeof(int32_t), st));
@@ -671,6 +707,25 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
         std::memcpy(L.lut, ctx->lut, sizeof L.lut);
     }
     CU(cudaStreamSynchronize(st));
+    if (resume) {
+        // The checkpoint's cut values against its spins, recomputed on the
+        // device (cutValueCsr, src/max_cut.cpp:5-15).
+        DevBuf d;
+        if ((rc = d.alloc(static_cast<size_t>(2 * C) * sizeof(int64_t)))) return rc;
+        CU(launch_chain_cuts(b->dChains.as<DevChain>(), b->dGraphs.as<DevGraph>(), static_cast<int>(C), 0,
+                             d.as<int64_t>(), st));
+        CU(launch_chain_cuts(b->dChains.as<DevChain>(), b->dGraphs.as<DevGraph>(), static_cast<int>(C), 1,
+                             d.as<int64_t>() + C, st));
+        std::vector<int64_t> cuts(static_cast<size_t>(2 * C));
+        CU(cudaMemcpyAsync(cuts.data(), d.p, cuts.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        for (int64_t i = 0; i < C; ++i)
+            if (cuts[i] != resume->cur_vals[i] || cuts[C + i] != resume->best_vals[i])
+                return fail(RFMF_ERR_INVALID,
+                            "checkpoint of chain %lld: cut values %lld / %lld, its spins give %lld / %lld",
+                            (long long)i, (long long)resume->cur_vals[i], (long long)resume->best_vals[i],
+                            (long long)cuts[i], (long long)cuts[C + i]);
+    }
     *out = b.release();
     return RFMF_OK;
 }
@@ -761,6 +816,7 @@ static int rfmf_batch_synchronize_impl(rfmf_batch* b) {
 static int rfmf_batch_read_impl(rfmf_batch* b, int8_t* end_spins, int8_t* best_spins,
                                int64_t* cur_vals, int64_t* best_vals, uint64_t* sweeps_done) {
     if (!b) return fail(RFMF_ERR_INVALID, "batch is NULL");
+    host_alloc_point();
     int rc = rfmf_batch_synchronize(b);
     if (rc) return rc;
     std::vector<DevChain> hc(b->C);
@@ -920,7 +976,158 @@ static int rfmf_anneal_impl(rfmf_context* ctx, const rfmf_graph* g, int64_t max_
     return rfmf_batch_read(b, end_spins, best_spins, kernel_final_vals, kernel_best_vals, nullptr);
 }
 
+// ---------------------------------------------------------------- autotune
+namespace {
+
+// The batch shape a tuned plan is cached under: per distinct graph its n, m,
+// B and chain count (sorted), the schedule, the trial length and the knobs
+// the caller fixed.
+std::string tune_key(int64_t C, const rfmf_graph* const* graphs, int64_t nphases, const uint64_t* phases,
+                     const uint64_t* iters, uint64_t trial, const rfmf_launch_config& base) {
+    std::map<const rfmf_graph*, int64_t> count;
+    for (int64_t i = 0; i < C; ++i) ++count[graphs[i]];
+    std::vector<std::tuple<int64_t, int64_t, int64_t, int64_t>> shape;
+    for (const auto& kv : count) shape.emplace_back(kv.first->n, kv.first->m, kv.first->B, kv.second);
+    std::sort(shape.begin(), shape.end());
+    std::string key;
+    char buf[96];
+    for (const auto& t : shape) {
+        std::snprintf(buf, sizeof buf, "g%lld,%lld,%lld,%lld;", (long long)std::get<0>(t), (long long)std::get<1>(t),
+                      (long long)std::get<2>(t), (long long)std::get<3>(t));
+        key += buf;
+    }
+    for (int64_t p = 0; p < nphases; ++p) {
+        std::snprintf(buf, sizeof buf, "p%llu,%llu;", (unsigned long long)phases[p], (unsigned long long)iters[p]);
+        key += buf;
+    }
+    std::snprintf(buf, sizeof buf, "t%llu;k%d,%d,%d,%d,%d", (unsigned long long)trial, base.threads_per_chain,
+                  base.csr_format, base.gain_width, base.score_path, base.chains_per_cta);
+    return key + buf;
+}
+
+}  // namespace
+
+static int rfmf_autotune_impl(rfmf_context* ctx, int64_t C, const rfmf_graph* const* graphs, const double* t0s,
+                              const uint64_t* solver_seeds, const int8_t* initial_spins, int64_t nphases,
+                              const uint64_t* phases, const uint64_t* iters, uint64_t trial_sweeps,
+                              const rfmf_launch_config* base, rfmf_launch_config* best, int* ncand,
+                              rfmf_launch_config* cand, float* cand_us) {
+    if (!ctx || !best || !graphs || C <= 0 || nphases < 0 || (nphases > 0 && (!phases || !iters)))
+        return fail(RFMF_ERR_INVALID, "bad arguments");
+    const rfmf_launch_config b0 = base ? *base : rfmf_launch_config{};
+    const uint64_t trial = trial_sweeps ? trial_sweeps : 512;
+    const std::string key = tune_key(C, graphs, nphases, phases, iters, trial, b0);
+    auto report = [&](const rfmf_context::TunedPlan& t) {
+        *best = t.best;
+        if (ncand) {
+            const int cap = *ncand;
+            *ncand = static_cast<int>(t.us.size());
+            for (int k = 0; k < static_cast<int>(t.us.size()) && k < cap; ++k) {
+                if (cand_us) cand_us[k] = t.us[k];
+                if (cand) cand[k] = t.cand[k];
+            }
+        }
+    };
+    {
+        std::lock_guard<std::mutex> lk(ctx->tuneMu);
+        auto it = ctx->tuneCache.find(key);
+        if (it != ctx->tuneCache.end()) {
+            report(it->second);
+            return RFMF_OK;
+        }
+    }
+    // The schedule compressed to `trial` sweeps, every phase keeping its share.
+    uint64_t total = 0;
+    for (int64_t p = 0; p < nphases; ++p)
+        if (phases[p]) total += iters[p];
+    std::vector<uint64_t> it(static_cast<size_t>(std::max<int64_t>(nphases, 1)), 0);
+    uint64_t tsum = 0;
+    for (int64_t p = 0; p < nphases; ++p) {
+        if (!phases[p] || !iters[p] || !total) continue;
+        it[p] = std::max<uint64_t>(1, static_cast<uint64_t>(std::llround(static_cast<double>(trial) * iters[p] / total)));
+        tsum += it[p];
+    }
+    if (!tsum) {   // nothing to time: the automatic plan
+        *best = b0;
+        if (ncand) *ncand = 0;
+        return RFMF_OK;
+    }
+    rfmf_context::TunedPlan tp;
+    for (int w : {0, 32, 64, 128}) {
+        if (b0.threads_per_chain && w != 0) continue;
+        for (int f : {0, 3}) {
+            if (b0.csr_format && f != 0) continue;
+            rfmf_launch_config c = b0;
+            if (w) c.threads_per_chain = w;
+            if (f) c.csr_format = f;
+            tp.cand.push_back(c);
+        }
+    }
+    int firstErr = RFMF_OK;
+    std::string firstMsg;
+    float bestUs = -1.0f;
+    for (const rfmf_launch_config& c : tp.cand) {
+        float fastest = -1.0f;
+        for (int rep = 0; rep < 2; ++rep) {
+            // Two windows of the trial schedule: the first warms the plan up
+            // and teaches it the graphs' costs (which size its work items),
+            // the second is timed.
+            rfmf_batch* tb = nullptr;
+            int rc = rfmf_batch_create(ctx, C, graphs, t0s, solver_seeds, initial_spins, nphases, phases,
+                                       it.data(), &c, &tb);
+            float ms = 0.0f, warm = 0.0f;
+            if (rc == RFMF_OK) rc = rfmf_batch_run_timed(tb, tsum, &warm);
+            if (tb) {
+                rfmf_batch_destroy(tb);
+                tb = nullptr;
+            }
+            if (rc == RFMF_OK)
+                rc = rfmf_batch_create(ctx, C, graphs, t0s, solver_seeds, initial_spins, nphases, phases,
+                                       it.data(), &c, &tb);
+            if (rc == RFMF_OK) rc = rfmf_batch_run_timed(tb, tsum, &ms);
+            if (tb) rfmf_batch_destroy(tb);
+            if (rc != RFMF_OK) {
+                if (!firstErr) { firstErr = rc; firstMsg = rfmf_last_error(); }
+                if (rc != RFMF_ERR_CAPACITY && rc != RFMF_ERR_INVALID) return rc;   // a CUDA failure is not a plan's fault
+                fastest = -1.0f;
+                break;
+            }
+            if (fastest < 0.0f || ms < fastest) fastest = ms;
+        }
+        const float us = fastest < 0.0f ? -1.0f
+                                        : static_cast<float>(fastest * 1e3 / (static_cast<double>(C) * tsum));
+        tp.us.push_back(us);
+        if (us >= 0.0f && (bestUs < 0.0f || us < bestUs)) {
+            bestUs = us;
+            tp.best = c;
+        }
+    }
+    if (bestUs < 0.0f) return fail(firstErr ? firstErr : RFMF_ERR_CAPACITY, "no candidate plan runs: %s", firstMsg.c_str());
+    {
+        std::lock_guard<std::mutex> lk(ctx->tuneMu);
+        ctx->tuneCache[key] = tp;
+    }
+    report(tp);
+    return RFMF_OK;
+}
+
 // C ABI entry points: no C++ exception crosses the boundary.
+extern "C" int rfmf_autotune(rfmf_context* ctx, int64_t nchains, const rfmf_graph* const* graphs,
+                             const double* t0s, const uint64_t* solver_seeds, const int8_t* initial_spins,
+                             int64_t nphases, const uint64_t* phases, const uint64_t* iters,
+                             uint64_t trial_sweeps, const rfmf_launch_config* base,
+                             rfmf_launch_config* best, int* ncand, rfmf_launch_config* cand,
+                             float* cand_us) {
+    try {
+        return rfmf_autotune_impl(ctx, nchains, graphs, t0s, solver_seeds, initial_spins, nphases, phases, iters,
+                                  trial_sweeps, base, best, ncand, cand, cand_us);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_autotune");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_autotune");
+    }
+}
+
 extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph* const* graphs,
                                  const double* t0s, const uint64_t* solver_seeds,
                                  const int8_t* initial_spins, int64_t nphases,
@@ -932,6 +1139,25 @@ extern "C" int rfmf_batch_create(rfmf_context* ctx, int64_t C, const rfmf_graph*
         return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_batch_create");
     } catch (...) {
         return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_batch_create");
+    }
+}
+
+extern "C" int rfmf_batch_restore(rfmf_context* ctx, int64_t nchains, const rfmf_graph* const* graphs,
+                                  const double* t0s, const uint64_t* solver_seeds, int64_t nphases,
+                                  const uint64_t* phases, const uint64_t* iters,
+                                  const rfmf_launch_config* cfg, const int8_t* end_spins,
+                                  const int8_t* best_spins, const int64_t* cur_vals,
+                                  const int64_t* best_vals, const uint64_t* sweeps_done, rfmf_batch** out) {
+    try {
+        if (!best_spins || !cur_vals || !best_vals || !sweeps_done)
+            return rfmf::fail(RFMF_ERR_INVALID, "NULL checkpoint array");
+        const Resume r{best_spins, cur_vals, best_vals, sweeps_done};
+        return rfmf_batch_create_impl(ctx, nchains, graphs, t0s, solver_seeds, end_spins, nphases, phases,
+                                      iters, cfg, out, &r);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_batch_restore");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_batch_restore");
     }
 }
 

@@ -15,13 +15,24 @@ struct alignas(8) Edge {
 };
 
 // How a launch reads the CSR.  The compact formats are copied once per CTA
-// into shared memory (bulk async copy) and walked there; kCsrGlobal walks the
-// 8-byte entries in HBM through L1/L2 (graphs too large for shared memory).
+// into shared memory (bulk async copy) and walked there; the HBM formats walk
+// the graph's own arrays through L1/L2 (graphs too large for shared memory
+// beside their chains), with the most compact entries the graph allows.
 enum CsrFormat : int32_t {
     kCsrUnit16 = 0,    // uint16 entry = (col << 1) | (w < 0); |w| == 1, n <= 32768
     kCsrPacked32 = 1,  // uint32 entry = (w << 16) | col;  |w| < 2^15, n <= 65536
     kCsrGlobal = 2,    // Edge {col, w} in HBM
+    kCsrGlobal16 = 3,  // the unit16 entries, in HBM
+    kCsrGlobal32 = 4,  // the packed32 entries, in HBM
 };
+
+#if defined(__CUDACC__)
+#define RFMF_CHD __host__ __device__ constexpr
+#else
+#define RFMF_CHD constexpr
+#endif
+// Formats walked in HBM (no shared-memory copy of the CSR).
+RFMF_CHD bool csr_in_hbm(int fmt) { return fmt == kCsrGlobal || fmt == kCsrGlobal16 || fmt == kCsrGlobal32; }
 
 // One CSR graph in HBM, read-only, shared by every chain that anneals it.
 // Rows are sorted ascending by neighbour (the reference's AnnealCsr order,

@@ -1,4 +1,4 @@
-// rfmf_host.cpp -- host side of librfmf.so: the C ABI of include/rfmf.h.
+// rfmf_driver.cpp -- host side of librfmf.so: the C ABI of include/rfmf.h.
 //
 // Replaces the reference's host driver (src/anneal_kernels.cu:498-884:
 // runDispatch/runMC/annealGpu) and the helpers of src/host_common.cpp it
@@ -20,6 +20,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/rfmf_testing.h"
 #include "rfmf_host.h"
 
 using namespace rfmf;
@@ -27,6 +28,7 @@ using namespace rfmf;
 namespace rfmf {
 
 thread_local std::string g_err;
+std::atomic<int64_t> g_allocCountdown{0};
 
 int fail(int code, const char* fmt, ...) {
     char buf[512];
@@ -284,6 +286,11 @@ bool score_safe_int32(int64_t total, double t0, int64_t B) {
 namespace rfmf {
 int set_last_error(int code, const char* msg) { return fail(code, "%s", msg); }
 }  // namespace rfmf
+
+extern "C" int rfmf_debug_fail_host_alloc(int64_t countdown) {
+    g_allocCountdown.store(countdown > 0 ? countdown : 0);
+    return RFMF_OK;
+}
 
 // ------------------------------------------------------------------ misc
 extern "C" const char* rfmf_version(void) { return "rfmf_gb300 0.1 (sm_103a)"; }

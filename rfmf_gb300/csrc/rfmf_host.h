@@ -6,12 +6,14 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
+#include <new>
 #include <string>
 #include <utility>
 #include <vector>
@@ -20,6 +22,20 @@
 #include "rfmf_device.h"
 
 namespace rfmf {
+
+// Host allocation checkpoint: throws std::bad_alloc when the countdown armed
+// by rfmf_debug_fail_host_alloc reaches it (a testing aid; a no-op
+// otherwise).
+extern std::atomic<int64_t> g_allocCountdown;
+inline void host_alloc_point() {
+    int64_t c = g_allocCountdown.load(std::memory_order_relaxed);
+    while (c > 0) {
+        if (g_allocCountdown.compare_exchange_weak(c, c - 1)) {
+            if (c == 1) throw std::bad_alloc();
+            return;
+        }
+    }
+}
 
 // Kernel entry points (rfmf_anneal.cu).
 const void* kernel_ptr(int dbytes, int fmt, bool s64);
@@ -243,6 +259,15 @@ struct rfmf_context {
     int64_t devBetaKeepBytes = 0;
     uint64_t devBetaUploads = 0;
     cudaStream_t uploadStream = nullptr;
+    // Measured plans (rfmf_autotune) by batch shape: the chosen config and
+    // every candidate's config and microseconds per chain-sweep.
+    struct TunedPlan {
+        rfmf_launch_config best;
+        std::vector<rfmf_launch_config> cand;
+        std::vector<float> us;
+    };
+    std::mutex tuneMu;
+    std::map<std::string, TunedPlan> tuneCache;
 };
 
 // A graph in device memory: offsets and 8-byte entries for HBM walks, plus
@@ -254,12 +279,42 @@ struct rfmf_graph {
     bool unit16 = false, packed32 = false;
     uint32_t offBytes = 0, u16Bytes = 0, p32Bytes = 0;
     rfmf::DevBuf offsets, edges, u16, p32;
-    // Learned cost: device ns per chain-sweep of one CTA slot, from the item
-    // timings of earlier launches (weight = chain-sweeps observed).  Feeds the
-    // work-item sizing of later launches; never affects results.
-    mutable double costNs = 0.0, costWeight = 0.0;
+    // Learned costs: device ns per chain-sweep of one CTA slot under a plan
+    // (warps per chain, CSR format), from the item timings of earlier
+    // launches (weight = chain-sweeps observed).  They size the work items of
+    // later launches of the same plan; they never affect results.
+    struct LearnedCost {
+        double ns = 0.0, weight = 0.0;
+    };
+    mutable std::map<std::pair<int, int>, LearnedCost> costs;
+    double cost(int warps, int fmt) const {
+        auto it = costs.find({warps, fmt});
+        return it == costs.end() ? 0.0 : it->second.ns;
+    }
+    void learn(int warps, int fmt, double ns, double weight) const {
+        LearnedCost& c = costs[{warps, fmt}];
+        c.ns = (c.ns * c.weight + ns * weight) / (c.weight + weight);
+        c.weight += weight;
+    }
     // Original vertex ids by dense id (graphs built from an edge list).
     std::vector<int64_t> origIds;
 };
+
+namespace rfmf {
+
+// The HBM-walk format of a graph: the most compact entries it has.
+inline int hbm_format(const rfmf_graph* g) {
+    return g->unit16 ? kCsrGlobal16 : (g->packed32 ? kCsrGlobal32 : kCsrGlobal);
+}
+
+// The entry array a launch of format `fmt` reads for graph g (the 8-byte
+// pairs are DevGraph::edges).
+inline const void* compact_entries(const rfmf_graph* g, int fmt) {
+    if (fmt == kCsrUnit16 || fmt == kCsrGlobal16) return g->u16.p;
+    if (fmt == kCsrPacked32 || fmt == kCsrGlobal32) return g->p32.p;
+    return nullptr;
+}
+
+}  // namespace rfmf
 
 #endif  // RFMF_HOST_H

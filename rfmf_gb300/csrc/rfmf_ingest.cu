@@ -179,6 +179,7 @@ static int rfmf_gset_parse_impl(const char* text, size_t len, double forced_scal
                                int64_t* u, int64_t* v, int64_t* w, int64_t* nedges,
                                double* scale_out, int64_t* zero_dropped) {
     if (!text || !u || !v || !w || !nedges) return fail(RFMF_ERR_INVALID, "NULL argument");
+    host_alloc_point();
     int64_t N = 0, M = 0;
     if (int rc = rfmf_gset_header(text, len, &N, &M)) return rc;
     if (cap < M) return fail(RFMF_ERR_CAPACITY, "cap %lld < %lld edges", (long long)cap, (long long)M);

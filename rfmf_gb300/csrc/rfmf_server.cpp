@@ -58,6 +58,7 @@ struct Request {
     int graphSlot = -1, schedSlot = -1;
     uint64_t done = 0;                // sweeps completed by every chain
     bool launched = false;
+    bool cancel = false;              // rfmf_cancel on a running request (under the server mutex)
     // status (under the server mutex)
     int state = RFMF_REQ_QUEUED;
     int error = RFMF_OK;
@@ -191,7 +192,7 @@ DevGraph dev_graph(const rfmf_graph* g, int fmt) {
     DevGraph d{};
     d.offsets = g->offsets.as<uint32_t>();
     d.edges = g->edges.as<Edge>();
-    d.compact = (fmt == kCsrUnit16) ? g->u16.p : (fmt == kCsrPacked32 ? g->p32.p : nullptr);
+    d.compact = compact_entries(g, fmt);
     d.n = static_cast<int32_t>(g->n);
     d.words = static_cast<int32_t>((g->n + 31) / 32);
     d.wsum2 = g->wsum2;
@@ -208,6 +209,7 @@ uint32_t csr_bytes(const rfmf_graph* g, int fmt) {
 
 // Device state of a newly admitted request (worker thread).
 int admit(rfmf_server* s, Request& r) {
+    host_alloc_point();
     const int64_t CW = r.C * r.words;
     int rc;
     if ((rc = r.dBits.alloc(CW * 4)) || (rc = r.dBest.alloc(CW * 4))) return rc;
@@ -321,6 +323,7 @@ void release(rfmf_server* s, Request& r) {
 
 // Copies a finished request's state to the host (worker thread).
 int harvest(rfmf_server* s, Request& r) {
+    host_alloc_point();
     const int64_t CW = r.C * r.words;
     r.endBits.resize(CW);
     r.bestBits.resize(CW);
@@ -489,6 +492,36 @@ void worker_main(rfmf_server* s) {
     }
 }
 
+// Host allocation failures inside admission, a window or a harvest become
+// a status, so the request in hand is failed instead of lost.
+template <class F>
+int nomem_safe(F&& f, const char* where) {
+    try {
+        return f();
+    } catch (const std::bad_alloc&) {
+        return fail(RFMF_ERR_NOMEM, "host allocation failed %s", where);
+    }
+}
+
+// Running requests that rfmf_cancel marked leave at this window boundary:
+// device state and slots freed, state CANCELLED (server mutex held, worker
+// thread, no launch in flight).
+void drop_cancelled(rfmf_server* s) {
+    bool any = false;
+    for (size_t i = 0; i < s->running.size();) {
+        Request& r = *s->running[i];
+        if (!r.cancel) { ++i; continue; }
+        release(s, r);
+        s->runningChains -= r.C;
+        s->runningBytes -= r.devBytes;
+        r.state = RFMF_REQ_CANCELLED;
+        r.finishS = s->now();
+        s->running.erase(s->running.begin() + static_cast<std::ptrdiff_t>(i));
+        any = true;
+    }
+    if (any) s->cvDone.notify_all();
+}
+
 void worker_loop(rfmf_server* s) {
     for (;;) {
         std::vector<ReqPtr> admitNow;
@@ -496,6 +529,7 @@ void worker_loop(rfmf_server* s) {
             std::unique_lock<std::mutex> lk(s->mu);
             s->cvWork.wait(lk, [&] { return s->stop || !s->queue.empty() || !s->running.empty(); });
             if (s->stop) break;
+            drop_cancelled(s);
             while (!s->queue.empty() &&
                    admits(s->runningChains, s->runningBytes, s->queue.front()->C,
                           s->queue.front()->devBytes, s->maxChains, s->maxDeviceBytes)) {
@@ -508,7 +542,7 @@ void worker_loop(rfmf_server* s) {
         }
         const auto w0 = Clock::now();
         for (ReqPtr& r : admitNow) {
-            const int rc = admit(s, *r);
+            const int rc = nomem_safe([&] { return admit(s, *r); }, "while admitting a request");
             std::lock_guard<std::mutex> lk(s->mu);
             if (rc != RFMF_OK) {
                 release(s, *r);
@@ -526,7 +560,7 @@ void worker_loop(rfmf_server* s) {
 
         int64_t launches = 0;
         float ms = 0.0f;
-        const int rc = run_window(s, launches, ms);
+        const int rc = nomem_safe([&] { return run_window(s, launches, ms); }, "in a launch window");
         std::vector<ReqPtr> finished;
         int64_t chainSweeps = 0;
         if (rc == RFMF_OK) {
@@ -540,7 +574,8 @@ void worker_loop(rfmf_server* s) {
         }
         std::string err = rc == RFMF_OK ? std::string() : std::string(rfmf_last_error());
         std::vector<std::pair<ReqPtr, int>> harvested;
-        for (ReqPtr& r : finished) harvested.push_back({r, harvest(s, *r)});
+        for (ReqPtr& r : finished)
+            harvested.push_back({r, nomem_safe([&] { return harvest(s, *r); }, "while reading results")});
         {
             std::lock_guard<std::mutex> lk(s->mu);
             const double t = s->now();
@@ -572,6 +607,7 @@ void worker_loop(rfmf_server* s) {
                 s->runningBytes -= r.devBytes;
                 s->running.erase(std::find(s->running.begin(), s->running.end(), h.first));
             }
+            drop_cancelled(s);
             s->cvDone.notify_all();
         }
     }
@@ -615,7 +651,7 @@ static int rfmf_server_create_impl(rfmf_context* ctx, const rfmf_server_config* 
         return fail(RFMF_ERR_INVALID, "threads_per_chain must be 0, 32, 64, 128 or 256");
     if (c.gain_width != 0 && c.gain_width != 1 && c.gain_width != 4)
         return fail(RFMF_ERR_INVALID, "gain_width must be 0, 1 or 4");
-    if (c.csr_format < 0 || c.csr_format > 3) return fail(RFMF_ERR_INVALID, "csr_format must be 0..3");
+    if (c.csr_format < 0 || c.csr_format > 4) return fail(RFMF_ERR_INVALID, "csr_format must be 0..4");
     if (c.score_path < 0 || c.score_path > 2) return fail(RFMF_ERR_INVALID, "score_path must be 0..2");
     CU(cudaSetDevice(ctx->device));
     CU(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
@@ -664,6 +700,7 @@ static int rfmf_submit_impl(rfmf_server* s, const rfmf_graph* g, int64_t nchains
     if (g->n == 0) return fail(RFMF_ERR_INVALID, "graph has no vertices");
     if (!initial_spins || !t0s || !solver_seeds || nphases < 0 || (nphases > 0 && (!phases || !iters)))
         return fail(RFMF_ERR_INVALID, "bad arguments");
+    host_alloc_point();
     auto r = std::make_shared<Request>();
     r->g = g;
     r->C = nchains;
@@ -722,10 +759,10 @@ static int rfmf_submit_impl(rfmf_server* s, const rfmf_graph* g, int64_t nchains
             return fail(RFMF_ERR_INVALID, "int32 scores would overflow for this (t0, B, sweeps)");
     }
     int fmt;
-    if (c.csr_format == 0) fmt = g->unit16 ? kCsrUnit16 : (g->packed32 ? kCsrPacked32 : kCsrGlobal);
+    if (c.csr_format == 0) fmt = g->unit16 ? kCsrUnit16 : (g->packed32 ? kCsrPacked32 : hbm_format(g));
     else if (c.csr_format == 1) { if (!g->unit16) return fail(RFMF_ERR_INVALID, "unit16 CSR needs |w| == 1 and n <= 32768"); fmt = kCsrUnit16; }
     else if (c.csr_format == 2) { if (!g->packed32) return fail(RFMF_ERR_INVALID, "packed32 CSR needs |w| < 2^15 and n <= 65536"); fmt = kCsrPacked32; }
-    else fmt = kCsrGlobal;
+    else fmt = (c.csr_format == 4) ? kCsrGlobal : hbm_format(g);
     // The shared CSR must leave room for about 8 warps of chains per CTA (or
     // the request's chains, if fewer), else the CSR is walked in HBM.
     {
@@ -735,9 +772,9 @@ static int rfmf_submit_impl(rfmf_server* s, const rfmf_graph* g, int64_t nchains
         const uint32_t chainB = chain_layout(static_cast<int>(g->n), static_cast<int>(r->words), r->pmax,
                                              r->W, r->dbytes).total;
         const int64_t kWant = std::min<int64_t>(nchains, std::max(1, 8 / r->W));
-        if (fmt != kCsrGlobal && static_cast<int64_t>(kSmemHeader) + csr_bytes(g, fmt) + kWant * chainB > dynMax) {
+        if (!csr_in_hbm(fmt) && static_cast<int64_t>(kSmemHeader) + csr_bytes(g, fmt) + kWant * chainB > dynMax) {
             if (c.csr_format != 0) return fail(RFMF_ERR_CAPACITY, "the shared-memory CSR does not fit");
-            fmt = kCsrGlobal;
+            fmt = hbm_format(g);
         }
         if (static_cast<int64_t>(kSmemHeader) + chainB > dynMax)
             return fail(RFMF_ERR_CAPACITY, "one chain needs %u B of shared memory", chainB);
@@ -775,7 +812,9 @@ static int rfmf_wait_impl(rfmf_server* s, uint64_t request_id, double timeout_s,
     auto it = s->all.find(request_id);
     if (it == s->all.end()) return fail(RFMF_ERR_INVALID, "unknown request %llu", static_cast<unsigned long long>(request_id));
     ReqPtr r = it->second;
-    auto ready = [&] { return r->state == RFMF_REQ_DONE || r->state == RFMF_REQ_FAILED; };
+    auto ready = [&] {
+        return r->state == RFMF_REQ_DONE || r->state == RFMF_REQ_FAILED || r->state == RFMF_REQ_CANCELLED;
+    };
     if (timeout_s < 0) {
         s->cvDone.wait(lk, ready);
     } else if (!s->cvDone.wait_for(lk, std::chrono::duration<double>(timeout_s), ready)) {
@@ -800,6 +839,10 @@ static int rfmf_result_impl(rfmf_server* s, uint64_t request_id, int8_t* end_spi
             s->all.erase(it);
             return fail(r->error, "request %llu failed: %s", static_cast<unsigned long long>(request_id), r->msg.c_str());
         }
+        if (r->state == RFMF_REQ_CANCELLED) {
+            s->all.erase(it);
+            return fail(RFMF_ERR_INVALID, "request %llu was cancelled", static_cast<unsigned long long>(request_id));
+        }
         if (r->state != RFMF_REQ_DONE)
             return fail(RFMF_ERR_INVALID, "request %llu is not done", static_cast<unsigned long long>(request_id));
         s->all.erase(it);
@@ -810,6 +853,27 @@ static int rfmf_result_impl(rfmf_server* s, uint64_t request_id, int8_t* end_spi
         if (best_vals) best_vals[c] = r->best[c];
         if (final_vals) final_vals[c] = r->cur[c];
     }
+    return RFMF_OK;
+}
+
+static int rfmf_cancel_impl(rfmf_server* s, uint64_t request_id) {
+    if (!s) return fail(RFMF_ERR_INVALID, "server is NULL");
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->all.find(request_id);
+        if (it == s->all.end()) return fail(RFMF_ERR_INVALID, "unknown request %llu", static_cast<unsigned long long>(request_id));
+        Request& r = *it->second;
+        if (r.state == RFMF_REQ_QUEUED) {
+            s->queue.erase(std::find(s->queue.begin(), s->queue.end(), it->second));
+            r.state = RFMF_REQ_CANCELLED;
+            r.finishS = s->now();
+            s->cvDone.notify_all();
+            return RFMF_OK;
+        }
+        if (r.state != RFMF_REQ_RUNNING) return RFMF_OK;   // finished: nothing to cancel
+        r.cancel = true;
+    }
+    s->cvWork.notify_one();
     return RFMF_OK;
 }
 
@@ -880,6 +944,16 @@ extern "C" int rfmf_poll(rfmf_server* s, uint64_t request_id, rfmf_request_statu
         return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_poll");
     } catch (...) {
         return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_poll");
+    }
+}
+
+extern "C" int rfmf_cancel(rfmf_server* s, uint64_t request_id) {
+    try {
+        return rfmf_cancel_impl(s, request_id);
+    } catch (const std::bad_alloc&) {
+        return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_cancel");
+    } catch (...) {
+        return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_cancel");
     }
 }
 

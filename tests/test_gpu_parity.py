@@ -64,7 +64,7 @@ def test_small_graphs_phases(rfmf, ctx, oracle, phases):
         assert_same(res, o, f"{g.name} {phases}")
 
 
-KNOBS = ([dict(csr_format=f, gain_width=w) for f in (1, 2, 3) for w in (1, 4)] +
+KNOBS = ([dict(csr_format=f, gain_width=w) for f in (1, 2, 3, 4) for w in (1, 4)] +
          [dict(threads_per_chain=t) for t in (64, 128, 256)] +
          [dict(chains_per_cta=k) for k in (1, 5)] +
          [dict(threads_per_chain=64, chains_per_cta=3, csr_format=3, gain_width=1),
@@ -80,6 +80,22 @@ def test_schedule_invariance(rfmf, ctx, oracle, knobs):
     res, o = run_pair(rfmf, ctx, oracle, g, [7, 8, 9], [70.0, 280.0, 35.0],
                       [128, 64, 32, 16, 8, 4, 2, 1, 3, 100], [30] * 10, cfg)
     assert_same(res, o, str(knobs))
+
+
+@pytest.mark.parametrize("fmt", [2, 3, 4])
+def test_weighted_graph_csr_formats(rfmf, ctx, oracle, fmt):
+    """Integer weights in [-5, 5]: the 32-bit entries staged in shared memory
+    (2), the same entries walked in HBM (3) and the 8-byte pairs in HBM (4)
+    give the oracle's results."""
+    rng = np.random.default_rng(17)
+    u = rng.integers(0, 500, 3000)
+    v = rng.integers(0, 500, 3000)
+    w = rng.integers(1, 6, 3000) * np.where(rng.random(3000) < 0.5, -1, 1)
+    g = rfmf.csr_from_edges(u, v, w, name="weighted500")
+    cfg = rfmf.make_config(csr_format=fmt)
+    res, o = run_pair(rfmf, ctx, oracle, g, [11, 12, 13, 14], [35.0, 70.0, 140.0, 280.0],
+                      [128, 16, 3, 1], [40] * 4, cfg)
+    assert_same(res, o, f"csr_format {fmt}")
 
 
 def test_er800_config1_shape(rfmf, ctx, oracle):

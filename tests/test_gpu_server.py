@@ -214,3 +214,75 @@ def test_device_beta_tables_shared_within_a_context(rfmf, ctx):
     dg.close()
     dref.close()
     c.close()
+
+
+def test_cancel_queued_and_running_requests(rfmf, ctx):
+    """rfmf_cancel: a queued request is cancelled at once and never starts; a
+    running one leaves at a window boundary, freeing its chains for the next
+    request; the others still equal their standalone anneals, and the
+    cancelled ones' results are refused."""
+    g = rfmf.erdos_renyi(500, 0.03, signed=True, seed=28)
+    dg = rfmf.DeviceGraph(ctx, g)
+    srv = rfmf.Server(ctx, window_sweeps=200, max_chains=64)
+    long_ = _request(rfmf, g, list(range(3100, 3164)), [35.0] * 64, [16, 1], [10**6, 10**6])
+    queued = _request(rfmf, g, list(range(3200, 3232)), [50.0] * 32, [8, 1], [400, 400])
+    short = _request(rfmf, g, list(range(3300, 3332)), [70.0] * 32, [8, 1], [400, 400])
+    ids = [srv.submit(dg, r["init"], r["t0s"], r["phases"], r["iters"], r["solver"])
+           for r in (long_, queued, short)]
+    import time
+    t_end = time.time() + 60
+    while srv.poll(ids[0])["state"] != "running" and time.time() < t_end:
+        time.sleep(0.01)
+    assert srv.poll(ids[0])["state"] == "running"
+    assert srv.poll(ids[1])["state"] == "queued"        # max_chains: 64 running
+    srv.cancel(ids[1])
+    st1 = srv.poll(ids[1])
+    assert st1["state"] == "cancelled" and st1["start_s"] == 0.0
+    srv.cancel(ids[0])
+    st0 = srv.wait(ids[0], timeout=120)
+    assert st0["state"] == "cancelled" and st0["sweeps_done"] < st0["sweeps_total"]
+    st2 = srv.wait(ids[2], timeout=300)
+    assert st2["state"] == "done"
+    _same(srv.result(ids[2]), _standalone(rfmf, ctx, dg, short))
+    for rid in ids[:2]:
+        with pytest.raises(rfmf.RfmfError):
+            srv.result(rid)
+    stats = srv.stats()
+    assert stats["queued"] == stats["running"] == 0
+    srv.close()
+
+
+def test_injected_host_allocation_failure_fails_one_request(rfmf, ctx):
+    """A host allocation failure while the worker admits a request fails that
+    request with RFMF_ERR_NOMEM (it is not lost: rfmf_wait returns); the
+    server keeps serving and the next request equals its standalone anneal.
+    The failure is injected on the host (rfmf_debug_fail_host_alloc), no GPU
+    fault is involved."""
+    g = rfmf.erdos_renyi(300, 0.04, signed=True, seed=29)
+    dg = rfmf.DeviceGraph(ctx, g)
+    srv = rfmf.Server(ctx, window_sweeps=300)
+    a = _request(rfmf, g, list(range(3400, 3408)), [35.0] * 8, [8, 1], [300, 300])
+    b = _request(rfmf, g, list(range(3500, 3508)), [50.0] * 8, [8, 1], [300, 300])
+    c = _request(rfmf, g, list(range(3600, 3608)), [70.0] * 8, [8, 1], [300, 300])
+    ra = srv.submit(dg, a["init"], a["t0s"], a["phases"], a["iters"], a["solver"])
+    assert srv.wait(ra, timeout=120)["state"] == "done"
+    _same(srv.result(ra), _standalone(rfmf, ctx, dg, a))
+    # checkpoint 1: rfmf_submit of b; checkpoint 2: b's admission in the worker
+    rfmf.debug_fail_host_alloc(2)
+    rb = srv.submit(dg, b["init"], b["t0s"], b["phases"], b["iters"], b["solver"])
+    stb = srv.wait(rb, timeout=120)
+    rfmf.debug_fail_host_alloc(0)
+    assert stb["state"] == "failed" and stb["error"] == 3, stb
+    with pytest.raises(rfmf.RfmfError) as ei:
+        srv.result(rb)
+    assert ei.value.code == 3
+    rc_ = srv.submit(dg, c["init"], c["t0s"], c["phases"], c["iters"], c["solver"])
+    assert srv.wait(rc_, timeout=120)["state"] == "done"
+    _same(srv.result(rc_), _standalone(rfmf, ctx, dg, c))
+    # a batch whose creation meets the failure reports it and nothing leaks
+    rfmf.debug_fail_host_alloc(1)
+    with pytest.raises(rfmf.RfmfError) as ei:
+        rfmf.Batch(ctx, [dg] * 8, c["t0s"], c["solver"], list(c["init"]), c["phases"], c["iters"])
+    rfmf.debug_fail_host_alloc(0)
+    assert ei.value.code == 3
+    srv.close()

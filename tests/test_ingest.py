@@ -97,3 +97,17 @@ def test_parser_matches_reference_loader_random(rfmf, ref_host, tmp_path):
         g = rfmf.csr_from_edges(d["u"], d["v"], d["w"])
         assert g.n == rn and np.array_equal(g.offsets, off), (case, mode)
         assert np.array_equal(g.col, col) and np.array_equal(g.weight, w), (case, mode)
+
+
+def test_injected_host_allocation_failure(rfmf):
+    """The testing aid rfmf_debug_fail_host_alloc makes the countdown-th host
+    allocation checkpoint fail; the call reports RFMF_ERR_NOMEM instead of
+    ending the process, and the next call works (host only: the parser)."""
+    text = "3 2\n1 2 1\n2 3 -1\n"
+    rfmf.debug_fail_host_alloc(2)
+    assert len(rfmf.parse_gset(text)["u"]) == 2          # first checkpoint passes
+    with pytest.raises(rfmf.RfmfError) as ei:
+        rfmf.parse_gset(text)                              # second one fails
+    assert ei.value.code == 3
+    assert len(rfmf.parse_gset(text)["u"]) == 2          # disarmed after firing
+    rfmf.debug_fail_host_alloc(0)
