@@ -288,7 +288,8 @@ def gpu_arm(args, rank, world):
         sweeps = (sweeps // q) * q
     per_step = sweeps // K
     phases, iters = schedule(sweeps, main_phases)
-    cfg = R.make_config(threads_per_chain=args.threads, chains_per_cta=args.chains_per_cta)
+    cfg = R.make_config(threads_per_chain=args.threads, chains_per_cta=args.chains_per_cta,
+                        csr_format=args.csr_format)
     base = rank * args.chains
     setup = chain_setup(graphs, args.chains, base)
     tuned = None
@@ -406,7 +407,7 @@ def gpu_arm(args, rank, world):
     serving_mixed = None
     if not args.no_serving:
         rates = [float(x) for x in str(args.serve_rate).split(",") if x]
-        runs = [serving_arm(args, ctx, r) for r in rates]
+        runs = [serving_arm(args, ctx, r, compare_offline=(r == rates[-1])) for r in rates]
         serving = runs[0] if len(runs) == 1 else runs
         budgets = [int(float(x)) for x in str(args.serve_budgets).split(",") if x]
         if budgets and args.serve_mixed_rate > 0:
@@ -818,7 +819,7 @@ def serving_graphs():
     return out
 
 
-def serving_arm(args, ctx, rate, budgets=None, max_requests=None):
+def serving_arm(args, ctx, rate, budgets=None, max_requests=None, compare_offline=False):
     """Continuous batching through the request server: Poisson arrivals at
     `rate` req/s for `seconds`, or until max_requests (default
     args.serve_max_requests) have arrived (which bounds the high-rate runs:
@@ -902,6 +903,24 @@ def serving_arm(args, ctx, rate, budgets=None, max_requests=None):
     wall = time.perf_counter() - t_start
     stats = srv.stats()
     srv.close()
+    # The same requests' chains as ONE offline batch (one schedule: only when
+    # every request has the same budget): what continuous batching costs
+    # against knowing the whole workload up front.
+    offline = None
+    if compare_offline and not budgets and args.serve_offline:
+        gl, ini, sol, t0 = [], [], [], []
+        for i, r in enumerate(reqs):
+            init, t0s, solver = inputs[i]
+            gl += [dgs[r["g"]]] * r["C"]
+            ini += list(init)
+            sol += solver
+            t0 += t0s
+        phases, iters = schedule(args.serve_sweeps)
+        b = R.Batch(ctx, gl, t0, sol, ini, phases, iters)
+        ms = b.run_timed(args.serve_sweeps)
+        b.close()
+        offline = {"chain_steps_per_s": len(ini) * args.serve_sweeps / (ms / 1e3), "kernel_ms": ms,
+                   "what": "every request's chains in one batch, one launch (device time)"}
     lat = np.array(lat)
     span = submitted[-1] - submitted[0] if len(submitted) > 1 else 0.0
     return {"rate_req_s": rate, "requests": len(reqs),
@@ -917,6 +936,8 @@ def serving_arm(args, ctx, rate, budgets=None, max_requests=None):
             "latency_max_s": float(lat.max()),
             "chain_steps_per_s": cs / wall, "wall_s": wall,
             "gpu_busy_frac": stats["kernel_s"] / wall, "windows": stats["windows"],
+            "kernel_chain_steps_per_s": stats["chain_sweeps"] / max(stats["kernel_s"], 1e-9),
+            "offline_batch_same_requests": offline,
             "launches": stats["launches"],
             "mix": "graphs torus/tree/ER-d5 at n 5000/10000/20000; chains 16-256 uniform over "
                    "{16,32,64,128,256}; Poisson arrivals"}
@@ -931,17 +952,30 @@ def e2e_arm(args, ctx, graphs, setup, per_step):
     import rfmf_gb300 as R
     phases, iters = schedule(per_step)
     K = min(args.steps, 2)
+    # Each call's plan measured once per shape, before the clock (a caller
+    # issuing many calls of one shape tunes once; the pick is cached in the
+    # context and passed as the call's launch config).
+    cfgs = []
+    for s in setup:
+        if args.no_autotune:
+            cfgs.append(R.make_config())
+            continue
+        dg = R.DeviceGraph(ctx, s["g"])
+        cfg, _ = R.autotune(ctx, [dg] * len(s["seeds"]), s["t0s"], s["solver"], list(s["init"]),
+                            phases, iters)
+        cfgs.append(cfg)
+        dg.close()
     h2d = d2h = 0
     t_graph = t_call = kern = 0.0
     t = time.perf_counter()
     for _ in range(K):
-        for s in setup:
+        for s, cfg in zip(setup, cfgs):
             g = s["g"]
             t1 = time.perf_counter()
             dg = R.DeviceGraph(ctx, g)
             t2 = time.perf_counter()
             res = R.anneal_gpu(ctx, dg, g.max_weighted_degree(), s["init"], s["t0s"], phases,
-                               iters, s["solver"])
+                               iters, s["solver"], cfg)
             t3 = time.perf_counter()
             dg.close()
             t_graph += t2 - t1
@@ -963,6 +997,8 @@ def e2e_arm(args, ctx, graphs, setup, per_step):
                             "anneal_call_other": t_call - kern,
                             "outside_calls": el - t_graph - t_call},
             "kernel_only_rate": chain_steps / kern,
+            "plans": [{"threads_per_chain": c.threads_per_chain, "csr_format": c.csr_format}
+                      for c in cfgs],
             "api": "rfmf_graph_create + rfmf_anneal (annealGpu drop-in), host buffers, one call "
                    f"per graph, {per_step} sweeps per chain per call"}
 
@@ -983,6 +1019,9 @@ def main():
                          "a profiling case (no e2e, CPU or plain-kernel legs)")
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--chains-per-cta", type=int, default=0)
+    ap.add_argument("--csr-format", type=int, default=0,
+                    help="0 auto; 1/2 shared-memory 16/32-bit entries; 3 HBM compact entries; "
+                         "4 HBM 8-byte entries (profiling cases)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="plan the batch with the planner's rules instead of measuring candidates")
@@ -1013,6 +1052,8 @@ def main():
     ap.add_argument("--serve-mixed-rate", type=float, default=10.0,
                     help="req/s of the mixed-budget serving run (0 = skip)")
     ap.add_argument("--serve-mixed-requests", type=int, default=40)
+    ap.add_argument("--serve-offline", type=int, default=1,
+                    help="also run each fixed-budget serving mix as one offline batch (1) or not (0)")
     args = ap.parse_args()
     if args.chains is None:
         args.chains = WORKLOAD_CHAINS[args.workload]
