@@ -50,6 +50,10 @@ const char* rfmf_last_error(void);
 /* Open a context on CUDA device `device`: replaces the cudaSetDevice and the
  * default-stream use of src/anneal_kernels.cu:874. */
 int rfmf_context_create(int device, rfmf_context** out);
+/* Release the caller's handle.  Graphs, batches and servers made on the
+ * context hold it too: its streams and tables go when the last of them is
+ * destroyed, so the order of the destroy calls does not matter.  The handle
+ * itself must not be used after this call. */
 int rfmf_context_destroy(rfmf_context* ctx);
 
 /* Device properties the autotuner uses (SM count, opt-in shared memory per
@@ -86,6 +90,9 @@ int rfmf_graph_create(rfmf_context* ctx, int64_t n, const uint32_t* offsets,
  * work); on success *max_weighted_degree (may be NULL) receives B. */
 int rfmf_csr_validate(int64_t n, const uint32_t* offsets, const int32_t* col,
                       const int32_t* weight, int64_t* max_weighted_degree);
+/* Release the caller's handle.  Batches and server requests on the graph
+ * hold it until they are destroyed or released; the handle itself must not
+ * be used after this call. */
 int rfmf_graph_destroy(rfmf_graph* g);
 
 /* n, m (undirected edges) and B = max weighted degree; any pointer may be NULL.

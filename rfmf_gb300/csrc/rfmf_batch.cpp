@@ -48,7 +48,8 @@ struct BatchClass {
     std::vector<DevItem> items;
     std::vector<int32_t> order;
     bool balanced = false;       // items sized from learned graph costs
-    uint64_t pendingSweeps = 0;  // sweeps of launches whose item times are unread
+    uint64_t pendingSweeps = 0;  // sweeps of the last launch, whose item times are unread
+    uint32_t pendingP = 0;       // its phase P (0: it spanned several phases)
     DevBuf dItems, dOrder, dItemNs, dCtl;
     DevLaunch L{};
     cudaStream_t stream = nullptr;
@@ -58,6 +59,8 @@ struct BatchClass {
 }  // namespace
 
 struct rfmf_batch {
+    rfmf::CtxHold ctxHold;   // first member: released last
+    rfmf::GraphHolds graphHolds;   // released after the device buffers
     rfmf_context* ctx = nullptr;
     int64_t C = 0;
     uint64_t total = 0;
@@ -65,6 +68,8 @@ struct rfmf_batch {
     std::vector<int64_t> graphOfChain;
     int64_t words = 0;                           // total spin words over chains
     std::vector<const rfmf_graph*> glist;
+    std::vector<uint32_t> phaseP;                // the schedule, host copy
+    std::vector<uint64_t> phaseIters;
     DevBuf dGraphs, dScheds, dChains, dPhaseP, dPhaseIters, dBits, dBest;
     std::vector<DevBetaRef> betaRefs;            // the context's shared beta tables in use
     std::vector<BatchClass> cls;
@@ -183,48 +188,53 @@ int plan_class(rfmf_batch& b, BatchClass& k, const rfmf_launch_config& c, bool e
     return RFMF_OK;
 }
 
-// Per-graph chains per item within a class.  With learned costs c_g (ns per
-// chain-sweep of a CTA slot) for every graph, pick the smallest per-sweep
-// makespan tau such that items of K_g = min(K, floor(tau / c_g)) chains all
-// fit the resident CTA slots; without costs every graph keeps its K.
-void plan_balanced(const rfmf_batch& b, BatchClass& k) {
+// Per-graph chains per item within a class, for phases of group count P.
+// With learned costs c_g (ns per chain-sweep of a CTA slot at P, or at the
+// nearest P learned) for every graph, pick the smallest per-sweep makespan
+// tau such that items of K_g = min(K, floor(tau / c_g)) chains all fit the
+// resident CTA slots.  False (kg untouched) when some graph has no cost yet
+// or no tau fits.
+bool plan_balanced(const rfmf_batch& b, const BatchClass& k, uint32_t P, std::vector<int>& kg) {
     const size_t G = k.graphs.size();
-    bool known = true;
-    for (int gi : k.graphs) known = known && b.glist[gi]->cost(k.warps, k.fmt) > 0.0;
-    if (!known || G < 2) { k.balanced = false; return; }
+    if (G < 2) return false;
+    std::vector<double> c(G);
+    for (size_t q = 0; q < G; ++q) {
+        c[q] = b.glist[k.graphs[q]]->cost(k.warps, k.fmt, P);
+        if (c[q] <= 0.0) return false;
+    }
     const int64_t slots = static_cast<int64_t>(k.occ) * b.ctx->sms;
     double lo = 0.0, hi = 0.0;
-    for (int gi : k.graphs) hi = std::max(hi, b.glist[gi]->cost(k.warps, k.fmt) * k.K);
-    auto fits = [&](double tau, std::vector<int>& kg) {
+    for (size_t q = 0; q < G; ++q) hi = std::max(hi, c[q] * k.K);
+    auto fits = [&](double tau, std::vector<int>& out) {
         int64_t items = 0;
         for (size_t q = 0; q < G; ++q) {
-            int v = static_cast<int>(std::floor(tau / b.glist[k.graphs[q]]->cost(k.warps, k.fmt)));
+            int v = static_cast<int>(std::floor(tau / c[q]));
             v = std::max(1, std::min(k.K, v));
-            kg[q] = v;
+            out[q] = v;
             items += (static_cast<int64_t>(k.chainsOf[q].size()) + v - 1) / v;
         }
         return items <= slots;
     };
-    std::vector<int> kg(G, k.K), best(G, k.K);
-    if (!fits(hi, kg)) { k.balanced = false; return; }
-    best = kg;
+    std::vector<int> trial(G, k.K), best(G, k.K);
+    if (!fits(hi, trial)) return false;
+    best = trial;
     for (int it = 0; it < 60; ++it) {
         const double mid = 0.5 * (lo + hi);
-        if (fits(mid, kg)) { hi = mid; best = kg; } else { lo = mid; }
+        if (fits(mid, trial)) { hi = mid; best = trial; } else { lo = mid; }
     }
-    k.Kg = best;
-    k.balanced = true;
+    kg = best;
+    return true;
 }
 
 // Items: graphs in decreasing per-item cost, each graph's chains in groups of
 // its K_g (item.graph is the batch graph index).
-void build_items(const rfmf_batch& b, BatchClass& k) {
+void build_items(const rfmf_batch& b, BatchClass& k, uint32_t P) {
     const size_t G = k.graphs.size();
     std::vector<int> gorder(G);
     for (size_t q = 0; q < G; ++q) gorder[q] = static_cast<int>(q);
     auto itemCost = [&](int q) {
         const rfmf_graph* g = b.glist[k.graphs[q]];
-        const double learned = g->cost(k.warps, k.fmt);
+        const double learned = g->cost(k.warps, k.fmt, P);
         const double c = learned > 0.0 ? learned : static_cast<double>(g->n);
         return c * k.Kg[q];
     };
@@ -258,9 +268,11 @@ int upload_items(rfmf_batch& b, BatchClass& k) {
 
 // Fold the item timings of completed launches into the graphs' costs.
 int harvest_item_times(rfmf_batch& b, BatchClass& k) {
-    if (!k.pendingSweeps || k.items.empty()) return RFMF_OK;
+    if (!k.pendingSweeps || !k.pendingP || k.items.empty()) return RFMF_OK;
     const uint64_t sweeps = k.pendingSweeps;
+    const uint32_t P = k.pendingP;
     k.pendingSweeps = 0;
+    k.pendingP = 0;
     std::vector<uint64_t> ns(k.items.size());
     CU(cudaMemcpy(ns.data(), k.dItemNs.p, ns.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
     for (size_t i = 0; i < k.items.size(); ++i) {
@@ -269,36 +281,56 @@ int harvest_item_times(rfmf_batch& b, BatchClass& k) {
         const double w = static_cast<double>(it.count) * static_cast<double>(sweeps);
         const double c = static_cast<double>(ns[i]) / w;
         const rfmf_graph* g = b.glist[it.graph];
-        g->learn(k.warps, k.fmt, c, w);
+        g->learn(k.warps, k.fmt, P, c, w);
     }
     return RFMF_OK;
 }
 
-// One window: every class's launch.  A single class goes out on the
-// context's stream; several are forked onto their own streams and joined
-// back, so run_timed events and graph capture see the whole window.
-// Re-size the work items of classes not yet balanced, once every graph of
-// the class has a learned cost (stream-ordered after older launches).
-int rebalance(rfmf_batch* b) {
+// The group count P of the phase that sweep `sweep` (0-based) falls in, and
+// the end of that phase (phases with P = 0 are skipped, as the kernel skips
+// them); past the schedule's end, the last phase with P > 0 and no end.
+uint32_t phase_at(const rfmf_batch& b, uint64_t sweep, uint64_t* end) {
+    uint64_t at = 0;
+    uint32_t last = 1;
+    for (size_t p = 0; p < b.phaseP.size(); ++p) {
+        if (!b.phaseP[p]) continue;
+        last = b.phaseP[p];
+        at += b.phaseIters[p];
+        if (sweep < at) {
+            *end = at;
+            return last;
+        }
+    }
+    *end = UINT64_MAX;
+    return last;
+}
+
+// Size the work items of multi-graph classes for phases of group count P
+// from the costs learned so far (re-planned before every launch: costs
+// keep arriving, and planning is a few microseconds per graph); uploaded
+// only when the per-graph item sizes change (stream-ordered after older
+// launches).  A class without costs for every graph keeps its items.
+int rebalance(rfmf_batch* b, uint32_t P) {
     for (BatchClass& k : b->cls) {
-        if (k.balanced) continue;
-        plan_balanced(*b, k);
-        if (k.balanced) {
-            build_items(*b, k);
+        if (k.graphs.size() < 2) continue;
+        std::vector<int> kg;
+        if (!plan_balanced(*b, k, P, kg)) continue;
+        const bool changed = !k.balanced || kg != k.Kg;
+        k.Kg = kg;
+        k.balanced = true;
+        if (changed) {
+            build_items(*b, k, P);
             if (int rc = upload_items(*b, k)) return rc;
         }
     }
     return RFMF_OK;
 }
 
-int enqueue_run(rfmf_batch* b, uint64_t sweeps, bool capturing = false) {
+// One launch per class over `sweeps` sweeps.  A single class goes out on
+// the context's stream; several are forked onto their own streams and
+// joined back, so run_timed events and graph capture see the whole window.
+int launch_window(rfmf_batch* b, uint64_t sweeps) {
     cudaStream_t main = b->ctx->stream;
-    if (!capturing) {
-        if (int rc = rebalance(b)) return rc;
-        const uint64_t adv = std::min<uint64_t>(sweeps, b->total - std::min(b->total, b->hostDone));
-        b->hostDone += adv;
-        for (BatchClass& k : b->cls) k.pendingSweeps = adv;
-    }
     const bool fork = b->cls.size() > 1;
     if (fork) CU(cudaEventRecord(b->fork, main));
     for (BatchClass& k : b->cls) {
@@ -312,6 +344,42 @@ int enqueue_run(rfmf_batch* b, uint64_t sweeps, bool capturing = false) {
             CU(cudaEventRecord(k.done, st));
             CU(cudaStreamWaitEvent(main, k.done, 0));
         }
+    }
+    return RFMF_OK;
+}
+
+// One window of `sweeps` sweeps.  When a class holds several graphs, whose
+// relative costs change with P, the window is cut at phase boundaries and
+// each piece runs with items sized for its phase; results do not depend on
+// the cut (a chain's sweeps are a function of its sweep index alone).
+int enqueue_run(rfmf_batch* b, uint64_t sweeps, bool capturing = false) {
+    if (capturing) return launch_window(b, sweeps);
+    uint64_t left = std::min<uint64_t>(sweeps, b->total - std::min(b->total, b->hostDone));
+    bool split = false;
+    for (const BatchClass& k : b->cls) split = split || k.graphs.size() > 1;
+    uint64_t end = 0;
+    const uint32_t P0 = phase_at(*b, b->hostDone, &end);
+    if (!split || left == 0 || left <= end - b->hostDone) {
+        if (int rc = rebalance(b, P0)) return rc;
+        const bool onePhase = left > 0 && left <= end - b->hostDone;
+        b->hostDone += left;
+        for (BatchClass& k : b->cls) {
+            k.pendingSweeps = left;
+            k.pendingP = onePhase ? P0 : 0;
+        }
+        return launch_window(b, sweeps);
+    }
+    while (left) {
+        const uint32_t P = phase_at(*b, b->hostDone, &end);
+        const uint64_t piece = std::min<uint64_t>(left, end - b->hostDone);
+        if (int rc = rebalance(b, P)) return rc;
+        b->hostDone += piece;
+        left -= piece;
+        for (BatchClass& k : b->cls) {
+            k.pendingSweeps = piece;
+            k.pendingP = P;
+        }
+        if (int rc = launch_window(b, piece)) return rc;
     }
     return RFMF_OK;
 }
@@ -367,9 +435,13 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
 
     auto b = std::unique_ptr<rfmf_batch>(new (std::nothrow) rfmf_batch());
     if (!b) return fail(RFMF_ERR_NOMEM, "host allocation failed");
+    b->ctxHold.set(ctx);
     b->ctx = ctx;
     b->C = C;
     b->total = total;
+    b->phaseP.assign(static_cast<size_t>(nphases), 0u);
+    b->phaseIters.assign(iters, iters + nphases);
+    for (int64_t p = 0; p < nphases; ++p) b->phaseP[p] = static_cast<uint32_t>(phases[p]);
 
     // Graph table (distinct graphs in first-use order).
     std::map<const rfmf_graph*, int> gidx;
@@ -379,6 +451,7 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
         if (it == gidx.end()) {
             it = gidx.emplace(graphs[i], static_cast<int>(b->glist.size())).first;
             b->glist.push_back(graphs[i]);
+            b->graphHolds.add(graphs[i]);
         }
         b->graphOfChain[i] = it->second;
     }
@@ -578,7 +651,11 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
         }
         if (rc) return rc;
     }
-    for (BatchClass& k : b->cls) build_items(*b, k);
+    {
+        uint64_t end = 0;
+        const uint32_t P0 = phase_at(*b, 0, &end);
+        for (BatchClass& k : b->cls) build_items(*b, k, P0);
+    }
 
     // Beta tables over the executed sweeps: the context's device copies,
     // shared with every other batch, call and request at the same (t0, sweeps).
@@ -741,8 +818,10 @@ static int rfmf_batch_run_graph_impl(rfmf_batch* b, uint64_t sweeps, int launche
     CU(cudaSetDevice(b->ctx->device));
     if (!b->graphExec || b->graphSweeps != sweeps || b->graphLaunches != launches) {
         if (b->graphExec) { cudaGraphExecDestroy(b->graphExec); b->graphExec = nullptr; }
-        // Items are sized before the capture (the graph replays them as they are).
-        if (int rc = rebalance(b)) return rc;
+        // Items are sized before the capture, for the phase the batch is in
+        // (the graph replays them as they are).
+        uint64_t end = 0;
+        if (int rc = rebalance(b, phase_at(*b, b->hostDone, &end))) return rc;
         cudaGraph_t graph = nullptr;
         CU(cudaStreamBeginCapture(b->ctx->stream, cudaStreamCaptureModeThreadLocal));
         int rc = RFMF_OK;

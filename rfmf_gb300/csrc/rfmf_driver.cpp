@@ -315,8 +315,9 @@ extern "C" int rfmf_context_create(int device, rfmf_context** out) {
     return RFMF_OK;
 }
 
-extern "C" int rfmf_context_destroy(rfmf_context* ctx) {
-    if (!ctx) return RFMF_OK;
+namespace rfmf {
+void let_go(rfmf_context* ctx) {
+    if (ctx->holders.fetch_sub(1) != 1) return;
     cudaSetDevice(ctx->device);
     {
         std::lock_guard<std::mutex> lk(ctx->devBetaMu);
@@ -326,6 +327,12 @@ extern "C" int rfmf_context_destroy(rfmf_context* ctx) {
     if (ctx->uploadStream) cudaStreamDestroy(ctx->uploadStream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
+}
+}  // namespace rfmf
+
+extern "C" int rfmf_context_destroy(rfmf_context* ctx) {
+    if (!ctx) return RFMF_OK;
+    let_go(ctx);
     return RFMF_OK;
 }
 
@@ -515,6 +522,7 @@ static int rfmf_graph_create_impl(rfmf_context* ctx, int64_t n, const uint32_t* 
     CU(cudaSetDevice(ctx->device));
     auto g = std::unique_ptr<rfmf_graph>(new (std::nothrow) rfmf_graph());
     if (!g) return fail(RFMF_ERR_NOMEM, "host allocation failed");
+    g->ctxHold.set(ctx);
     g->ctx = ctx;
     g->n = n;
     g->m = static_cast<int64_t>(m2 / 2);
@@ -558,10 +566,17 @@ static int rfmf_graph_create_impl(rfmf_context* ctx, int64_t n, const uint32_t* 
     return RFMF_OK;
 }
 
-extern "C" int rfmf_graph_destroy(rfmf_graph* g) {
-    if (!g) return RFMF_OK;
+namespace rfmf {
+void let_go(const rfmf_graph* g) {
+    if (g->holders.fetch_sub(1) != 1) return;
     cudaSetDevice(g->ctx->device);
     delete g;
+}
+}  // namespace rfmf
+
+extern "C" int rfmf_graph_destroy(rfmf_graph* g) {
+    if (!g) return RFMF_OK;
+    let_go(g);
     return RFMF_OK;
 }
 
@@ -589,6 +604,13 @@ int choose_warps(int maxN, const rfmf_launch_config& c, int64_t chains, int sms)
     // warps buy (GB300, 256 chains of ER n = 2000: 67.5 -> 88.6 M
     // chain-steps/s from one warp to four; 32 chains of ER n = 800: 6.7 -> 11.0).
     while (W < kMaxAutoWarps && chains > 0 && chains * 2 * W <= int64_t(8) * sms && nblk >= 32 * W)
+        W *= 2;
+    // Past four warps only for large graphs, where each thread keeps at
+    // least four vertex blocks (GB300, 32-64 chains: torus n = 20000 +15% at
+    // P = 128 and +29% at P = 1 from four warps to eight, tree n = 10000 +2%
+    // / +10%; ER n = 5000 -1% / +5%, so it stays at four).
+    while (W >= kMaxAutoWarps && W < kMaxLatencyWarps && chains > 0 && chains * 2 * W <= int64_t(8) * sms &&
+           nblk >= 256 * W)
         W *= 2;
     return W;
 }

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <deque>
@@ -15,6 +16,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -96,6 +98,7 @@ bool score_safe_int32(int64_t total, double t0, int64_t B);
 // Warps per chain: at least one per ~768 vertex blocks, more while the batch's
 // `chains` leave the SMs (`sms`) short of work; c.threads_per_chain overrides.
 constexpr int kMaxAutoWarps = 4;
+constexpr int kMaxLatencyWarps = 8;   // widest chain the planner picks for few chains
 int choose_warps(int maxN, const rfmf_launch_config& c, int64_t chains, int sms);
 int key_bits(int64_t n, int T);
 bool compact_key_safe(int64_t total, double t0, int64_t B, int kb);
@@ -268,31 +271,74 @@ struct rfmf_context {
     };
     std::mutex tuneMu;
     std::map<std::string, TunedPlan> tuneCache;
+    // Holders: the caller's handle plus every graph, batch and server made
+    // on the context.  The context is torn down when the last one lets go,
+    // so rfmf_context_destroy may come before theirs (a garbage collector
+    // finalises objects in any order).
+    std::atomic<int> holders{1};
 };
+
+namespace rfmf {
+// Drop one hold on ctx; the last one destroys its streams and tables.
+void let_go(rfmf_context* ctx);
+
+// A graph's, batch's or server's hold on its context.  Declared as the
+// object's first member, it is released after every other member (device
+// buffers, shared beta tables) is gone.
+struct CtxHold {
+    rfmf_context* ctx = nullptr;
+    CtxHold() = default;
+    CtxHold(const CtxHold&) = delete;
+    CtxHold& operator=(const CtxHold&) = delete;
+    void set(rfmf_context* c) {
+        if (ctx) let_go(ctx);
+        ctx = c;
+        if (c) c->holders.fetch_add(1);
+    }
+    ~CtxHold() {
+        if (ctx) let_go(ctx);
+    }
+};
+}  // namespace rfmf
 
 // A graph in device memory: offsets and 8-byte entries for HBM walks, plus
 // the compact entry arrays the shared-memory formats stage from (present
 // when the graph qualifies).  All arrays are padded to 16 bytes.
 struct rfmf_graph {
+    rfmf::CtxHold ctxHold;   // first member: released last
     rfmf_context* ctx = nullptr;
+    // Holders: the caller's handle plus every batch and request that runs
+    // on the graph; freed when the last one lets go.
+    mutable std::atomic<int> holders{1};
     int64_t n = 0, m = 0, B = 0, wsum2 = 0;
     bool unit16 = false, packed32 = false;
     uint32_t offBytes = 0, u16Bytes = 0, p32Bytes = 0;
     rfmf::DevBuf offsets, edges, u16, p32;
     // Learned costs: device ns per chain-sweep of one CTA slot under a plan
-    // (warps per chain, CSR format), from the item timings of earlier
-    // launches (weight = chain-sweeps observed).  They size the work items of
-    // later launches of the same plan; they never affect results.
+    // (warps per chain, CSR format) in phases of group count P, from the item
+    // timings of earlier launches (weight = chain-sweeps observed).  The
+    // relative cost of two graphs depends on P (at P = 128 a dense graph's
+    // row walks double its sweep; at P = 1 its vertex count decides), so
+    // they are kept per P.  They size the work items of later launches of
+    // the same plan; they never affect results.
     struct LearnedCost {
         double ns = 0.0, weight = 0.0;
     };
-    mutable std::map<std::pair<int, int>, LearnedCost> costs;
-    double cost(int warps, int fmt) const {
-        auto it = costs.find({warps, fmt});
-        return it == costs.end() ? 0.0 : it->second.ns;
+    mutable std::map<std::tuple<int, int, uint32_t>, LearnedCost> costs;
+    // The cost at phase P; without one, the cost learned at the nearest P
+    // (in log2 P) under the same plan; 0 when the plan has none.
+    double cost(int warps, int fmt, uint32_t P) const {
+        double best = 0.0, dist = 1e300;
+        const double lp = std::log2(static_cast<double>(P > 0 ? P : 1));
+        for (auto it = costs.lower_bound({warps, fmt, 0u});
+             it != costs.end() && std::get<0>(it->first) == warps && std::get<1>(it->first) == fmt; ++it) {
+            const double d = std::fabs(std::log2(static_cast<double>(std::get<2>(it->first))) - lp);
+            if (d < dist) { dist = d; best = it->second.ns; }
+        }
+        return best;
     }
-    void learn(int warps, int fmt, double ns, double weight) const {
-        LearnedCost& c = costs[{warps, fmt}];
+    void learn(int warps, int fmt, uint32_t P, double ns, double weight) const {
+        LearnedCost& c = costs[{warps, fmt, P > 0 ? P : 1u}];
         c.ns = (c.ns * c.weight + ns * weight) / (c.weight + weight);
         c.weight += weight;
     }
@@ -301,6 +347,25 @@ struct rfmf_graph {
 };
 
 namespace rfmf {
+
+// Drop one hold on g; the last one frees it.
+void let_go(const rfmf_graph* g);
+
+// The holds a batch or a request keeps on the graphs it runs on, released
+// when it is destroyed (so a graph destroyed first stays valid meanwhile).
+struct GraphHolds {
+    std::vector<const rfmf_graph*> held;
+    GraphHolds() = default;
+    GraphHolds(const GraphHolds&) = delete;
+    GraphHolds& operator=(const GraphHolds&) = delete;
+    void add(const rfmf_graph* g) {
+        g->holders.fetch_add(1);
+        held.push_back(g);
+    }
+    ~GraphHolds() {
+        for (const rfmf_graph* g : held) let_go(g);
+    }
+};
 
 // The HBM-walk format of a graph: the most compact entries it has.
 inline int hbm_format(const rfmf_graph* g) {

@@ -518,6 +518,7 @@ static int rfmf_graph_from_edges_impl(rfmf_context* ctx, int64_t nedges, const i
 
     auto g = std::unique_ptr<rfmf_graph>(new (std::nothrow) rfmf_graph());
     if (!g) return fail(RFMF_ERR_NOMEM, "host allocation failed");
+    g->ctxHold.set(ctx);
     g->ctx = ctx;
     g->n = n;
     g->m = m2 / 2;

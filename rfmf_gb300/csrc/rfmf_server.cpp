@@ -37,6 +37,7 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 struct Request {
+    GraphHolds graphHold;   // first member: released last
     uint64_t id = 0;
     const rfmf_graph* g = nullptr;
     int64_t C = 0, n = 0, words = 0;
@@ -119,6 +120,7 @@ struct ClassKey {
 }  // namespace
 
 struct rfmf_server {
+    rfmf::CtxHold ctxHold;   // first member: released last
     rfmf_context* ctx = nullptr;
     uint64_t window = 4096;
     int64_t maxChains = int64_t(1) << 20;
@@ -636,6 +638,7 @@ static int rfmf_server_create_impl(rfmf_context* ctx, const rfmf_server_config* 
     *out = nullptr;
     auto s = std::unique_ptr<rfmf_server>(new (std::nothrow) rfmf_server());
     if (!s) return fail(RFMF_ERR_NOMEM, "host allocation failed");
+    s->ctxHold.set(ctx);
     s->ctx = ctx;
     if (cfg) {
         if (cfg->window_sweeps) s->window = cfg->window_sweeps;
@@ -703,6 +706,7 @@ static int rfmf_submit_impl(rfmf_server* s, const rfmf_graph* g, int64_t nchains
     host_alloc_point();
     auto r = std::make_shared<Request>();
     r->g = g;
+    r->graphHold.add(g);
     r->C = nchains;
     r->n = g->n;
     r->words = (g->n + 31) / 32;

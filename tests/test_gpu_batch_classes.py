@@ -99,3 +99,58 @@ def test_widening_when_shared_memory_limits_residency(rfmf, ctx):
         b.close()
     assert widths[16 * sms] == 64, widths
     assert widths[8 * sms] == 32, widths
+
+
+def test_items_resized_per_phase_keep_results(rfmf, ctx, oracle):
+    """Two graphs in one class whose relative cost flips between phases (a
+    dense ER graph costs more per sweep at P = 128, the larger torus at
+    P = 1): windows that cross phase boundaries are cut there and each piece
+    runs with items sized from costs learned at its own P (synchronised
+    windows, so costs are learned between them).  Every chain still equals
+    the oracle."""
+    graphs = [rfmf.torus(30, 30, signed=True, seed=4), rfmf.erdos_renyi(600, 0.05, signed=True, seed=5)]
+    phases, iters = [128, 16, 1], [120, 120, 120]
+    dgs = [rfmf.DeviceGraph(ctx, g) for g in graphs]
+    gl, ini, sol, t0, per = [], [], [], [], []
+    for k, g in enumerate(graphs):
+        init, solver = chains_for(g, list(range(500 * k, 500 * k + 96)))
+        ts = [35.0 + 15 * (i % 8) for i in range(96)]
+        per.append((init, solver, ts))
+        gl += [dgs[k]] * 96
+        ini += list(init)
+        sol += solver
+        t0 += ts
+    b = rfmf.Batch(ctx, gl, t0, sol, ini, phases, iters)
+    assert b.info()["launch_classes"] == 1
+    for _ in range(4):
+        b.run_timed(90)
+    info = b.info()
+    r = b.read()
+    b.close()
+    assert info["balanced"] == 1, info
+    for k, g in enumerate(graphs):
+        init, solver, ts = per[k]
+        ref = oracle.anneal(g, init, ts, solver, phases, iters)
+        sl = slice(96 * k, 96 * k + 96)
+        assert np.array_equal(np.stack(r["end_spins"][sl]), ref["end_spins"]), k
+        assert np.array_equal(np.stack(r["best_spins"][sl]), ref["best_spins"]), k
+        assert np.array_equal(r["cur_vals"][sl], ref["cur_vals"]), k
+        assert np.array_equal(r["best_vals"][sl], ref["best_vals"]), k
+    for dg in dgs:
+        dg.close()
+
+
+def test_few_chains_of_a_large_graph_get_eight_warps(rfmf, ctx):
+    """32 chains of a 100x200 torus (n = 20000) run eight warps per chain;
+    32 chains of ER n = 5000 stay at four (the plan; results do not depend
+    on the width)."""
+    widths = {}
+    for name, g in (("torus", rfmf.torus(100, 200, signed=True, seed=0)),
+                    ("er", rfmf.erdos_renyi_sparse(5000, 5, signed=True, seed=0))):
+        dg = rfmf.DeviceGraph(ctx, g)
+        init, solver = chains_for(g, list(range(32)))
+        b = rfmf.Batch(ctx, [dg] * 32, [70.0] * 32, solver, list(init), [8, 1], [4, 4])
+        widths[name] = b.info()["threads_per_chain"]
+        b.close()
+        dg.close()
+    assert widths == {"torus": 256, "er": 128}, widths
