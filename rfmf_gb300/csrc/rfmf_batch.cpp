@@ -36,6 +36,8 @@ using namespace rfmf;
 
 namespace {
 
+constexpr uint64_t kMinLearnSweeps = 256;
+
 // Chains whose graphs share a kernel variant and a CTA layout.
 struct BatchClass {
     bool score64 = false;
@@ -189,40 +191,50 @@ int plan_class(rfmf_batch& b, BatchClass& k, const rfmf_launch_config& c, bool e
 }
 
 // Per-graph chains per item within a class, for phases of group count P.
-// With learned costs c_g (ns per chain-sweep of a CTA slot at P, or at the
-// nearest P learned) for every graph, pick the smallest per-sweep makespan
-// tau such that items of K_g = min(K, floor(tau / c_g)) chains all fit the
-// resident CTA slots.  False (kg untouched) when some graph has no cost yet
-// or no tau fits.
+// An item's time per sweep depends on its graph and its scheduler level
+// (sched_level), so each graph's candidates are the largest chain count of
+// each level up to the class's K.  With learned costs for every graph, the
+// smallest makespan tau whose items all fit the resident CTA slots wins,
+// each graph taking its largest candidate with cost <= tau.  False (kg
+// untouched) when some graph has no cost yet or nothing fits.
 bool plan_balanced(const rfmf_batch& b, const BatchClass& k, uint32_t P, std::vector<int>& kg) {
     const size_t G = k.graphs.size();
     if (G < 2) return false;
-    std::vector<double> c(G);
+    struct Cand { int K; double ns; };
+    std::vector<std::vector<Cand>> cand(G);
+    std::vector<double> taus;
     for (size_t q = 0; q < G; ++q) {
-        c[q] = b.glist[k.graphs[q]]->cost(k.warps, k.fmt, P);
-        if (c[q] <= 0.0) return false;
+        const rfmf_graph* g = b.glist[k.graphs[q]];
+        for (int K = 1; K <= k.K; ++K) {
+            if (K < k.K && sched_level(K + 1, k.warps) == sched_level(K, k.warps)) continue;
+            const double c = g->cost(k.warps, k.fmt, P, sched_level(K, k.warps));
+            if (c <= 0.0) return false;
+            cand[q].push_back({K, c});
+            taus.push_back(c);
+        }
     }
     const int64_t slots = static_cast<int64_t>(k.occ) * b.ctx->sms;
-    double lo = 0.0, hi = 0.0;
-    for (size_t q = 0; q < G; ++q) hi = std::max(hi, c[q] * k.K);
-    auto fits = [&](double tau, std::vector<int>& out) {
+    std::sort(taus.begin(), taus.end());
+    auto pick = [&](double tau, std::vector<int>& out) {
         int64_t items = 0;
         for (size_t q = 0; q < G; ++q) {
-            int v = static_cast<int>(std::floor(tau / c[q]));
-            v = std::max(1, std::min(k.K, v));
-            out[q] = v;
-            items += (static_cast<int64_t>(k.chainsOf[q].size()) + v - 1) / v;
+            int K = 0;
+            for (const Cand& c : cand[q])
+                if (c.ns <= tau) K = c.K;
+            if (!K) return false;
+            out[q] = K;
+            items += (static_cast<int64_t>(k.chainsOf[q].size()) + K - 1) / K;
         }
         return items <= slots;
     };
-    std::vector<int> trial(G, k.K), best(G, k.K);
-    if (!fits(hi, trial)) return false;
-    best = trial;
-    for (int it = 0; it < 60; ++it) {
-        const double mid = 0.5 * (lo + hi);
-        if (fits(mid, trial)) { hi = mid; best = trial; } else { lo = mid; }
+    std::vector<int> trial(G, 0);
+    size_t lo = 0, hi = taus.size();   // first feasible index in [lo, hi)
+    while (lo < hi) {
+        const size_t mid = (lo + hi) / 2;
+        if (pick(taus[mid], trial)) hi = mid; else lo = mid + 1;
     }
-    kg = best;
+    if (lo == taus.size() || !pick(taus[lo], trial)) return false;
+    kg = trial;
     return true;
 }
 
@@ -234,9 +246,8 @@ void build_items(const rfmf_batch& b, BatchClass& k, uint32_t P) {
     for (size_t q = 0; q < G; ++q) gorder[q] = static_cast<int>(q);
     auto itemCost = [&](int q) {
         const rfmf_graph* g = b.glist[k.graphs[q]];
-        const double learned = g->cost(k.warps, k.fmt, P);
-        const double c = learned > 0.0 ? learned : static_cast<double>(g->n);
-        return c * k.Kg[q];
+        const double learned = g->cost(k.warps, k.fmt, P, sched_level(k.Kg[q], k.warps));
+        return learned > 0.0 ? learned : static_cast<double>(g->n) * k.Kg[q];
     };
     std::stable_sort(gorder.begin(), gorder.end(), [&](int a, int z) { return itemCost(a) > itemCost(z); });
     k.items.clear();
@@ -267,6 +278,9 @@ int upload_items(rfmf_batch& b, BatchClass& k) {
 }
 
 // Fold the item timings of completed launches into the graphs' costs.
+// Launches shorter than kMinLearnSweeps teach nothing: an item's time also
+// holds its CSR staging and its chains' state load and gain set-up, which
+// would dominate a short window and differ by graph.
 int harvest_item_times(rfmf_batch& b, BatchClass& k) {
     if (!k.pendingSweeps || !k.pendingP || k.items.empty()) return RFMF_OK;
     const uint64_t sweeps = k.pendingSweeps;
@@ -275,13 +289,13 @@ int harvest_item_times(rfmf_batch& b, BatchClass& k) {
     k.pendingP = 0;
     std::vector<uint64_t> ns(k.items.size());
     CU(cudaMemcpy(ns.data(), k.dItemNs.p, ns.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    if (sweeps < kMinLearnSweeps) return RFMF_OK;
     for (size_t i = 0; i < k.items.size(); ++i) {
         const DevItem& it = k.items[i];
         if (ns[i] == 0 || it.count <= 0) continue;
-        const double w = static_cast<double>(it.count) * static_cast<double>(sweeps);
-        const double c = static_cast<double>(ns[i]) / w;
+        const double w = static_cast<double>(sweeps);
         const rfmf_graph* g = b.glist[it.graph];
-        g->learn(k.warps, k.fmt, P, c, w);
+        g->learn(k.warps, k.fmt, P, sched_level(std::min(it.count, k.K), k.warps), static_cast<double>(ns[i]) / w, w);
     }
     return RFMF_OK;
 }

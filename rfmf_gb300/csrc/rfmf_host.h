@@ -9,6 +9,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -99,6 +100,9 @@ bool score_safe_int32(int64_t total, double t0, int64_t B);
 // `chains` leave the SMs (`sms`) short of work; c.threads_per_chain overrides.
 constexpr int kMaxAutoWarps = 4;
 constexpr int kMaxLatencyWarps = 8;   // widest chain the planner picks for few chains
+// Warps an item of `chains` chains of `warps` warps each puts on one of the
+// SM's four schedulers (warp w issues from scheduler w mod 4).
+inline int sched_level(int chains, int warps) { return (chains * warps + 3) / 4; }
 int choose_warps(int maxN, const rfmf_launch_config& c, int64_t chains, int sms);
 int key_bits(int64_t n, int T);
 bool compact_key_safe(int64_t total, double t0, int64_t B, int kb);
@@ -314,31 +318,46 @@ struct rfmf_graph {
     bool unit16 = false, packed32 = false;
     uint32_t offBytes = 0, u16Bytes = 0, p32Bytes = 0;
     rfmf::DevBuf offsets, edges, u16, p32;
-    // Learned costs: device ns per chain-sweep of one CTA slot under a plan
-    // (warps per chain, CSR format) in phases of group count P, from the item
-    // timings of earlier launches (weight = chain-sweeps observed).  The
-    // relative cost of two graphs depends on P (at P = 128 a dense graph's
-    // row walks double its sweep; at P = 1 its vertex count decides), so
-    // they are kept per P.  They size the work items of later launches of
-    // the same plan; they never affect results.
+    // Learned costs: device time per sweep of one work item, by plan (warps
+    // per chain, CSR format), phase group count P and scheduler level (the
+    // warps an item puts on each of the SM's four schedulers,
+    // sched_level), from the item timings of earlier launches (weight =
+    // sweeps observed).  An item's chains run at the pace of its busiest
+    // scheduler: on GB300, 13 to 16 one-warp chains of the 50x60 torus take
+    // 4.53 us per sweep at P = 1 and 12 take 3.74; and two graphs' relative
+    // cost depends on P (at P = 128 a dense graph's row walks double its
+    // sweep; at P = 1 its vertex count decides).  They size the work items
+    // of later launches of the same plan; they never affect results.
     struct LearnedCost {
         double ns = 0.0, weight = 0.0;
     };
-    mutable std::map<std::tuple<int, int, uint32_t>, LearnedCost> costs;
-    // The cost at phase P; without one, the cost learned at the nearest P
-    // (in log2 P) under the same plan; 0 when the plan has none.
-    double cost(int warps, int fmt, uint32_t P) const {
-        double best = 0.0, dist = 1e300;
+    mutable std::map<std::tuple<int, int, uint32_t, int>, LearnedCost> costs;
+    // The item time per sweep at (plan, P, level): from the nearest P (in
+    // log2 P) learned under the plan, at the nearest level learned there,
+    // scaled to `level` by (level + 3) / (learned level + 3) (measured
+    // level-4 / level-3 ratios 1.11 to 1.21); 0 when the plan has none.
+    double cost(int warps, int fmt, uint32_t P, int level) const {
         const double lp = std::log2(static_cast<double>(P > 0 ? P : 1));
-        for (auto it = costs.lower_bound({warps, fmt, 0u});
+        double pd = 1e300;
+        uint32_t bestP = 0;
+        for (auto it = costs.lower_bound({warps, fmt, 0u, 0});
              it != costs.end() && std::get<0>(it->first) == warps && std::get<1>(it->first) == fmt; ++it) {
             const double d = std::fabs(std::log2(static_cast<double>(std::get<2>(it->first))) - lp);
-            if (d < dist) { dist = d; best = it->second.ns; }
+            if (d < pd) { pd = d; bestP = std::get<2>(it->first); }
         }
-        return best;
+        if (!bestP) return 0.0;
+        int bestL = 0;
+        double ns = 0.0;
+        for (auto it = costs.lower_bound({warps, fmt, bestP, 0});
+             it != costs.end() && std::get<0>(it->first) == warps && std::get<1>(it->first) == fmt &&
+             std::get<2>(it->first) == bestP; ++it) {
+            const int L = std::get<3>(it->first);
+            if (!bestL || std::abs(L - level) < std::abs(bestL - level)) { bestL = L; ns = it->second.ns; }
+        }
+        return ns * (level + 3.0) / (bestL + 3.0);
     }
-    void learn(int warps, int fmt, uint32_t P, double ns, double weight) const {
-        LearnedCost& c = costs[{warps, fmt, P > 0 ? P : 1u}];
+    void learn(int warps, int fmt, uint32_t P, int level, double ns, double weight) const {
+        LearnedCost& c = costs[{warps, fmt, P > 0 ? P : 1u, level}];
         c.ns = (c.ns * c.weight + ns * weight) / (c.weight + weight);
         c.weight += weight;
     }

@@ -106,10 +106,10 @@ def test_items_resized_per_phase_keep_results(rfmf, ctx, oracle):
     dense ER graph costs more per sweep at P = 128, the larger torus at
     P = 1): windows that cross phase boundaries are cut there and each piece
     runs with items sized from costs learned at its own P (synchronised
-    windows, so costs are learned between them).  Every chain still equals
-    the oracle."""
+    windows of 300 sweeps, so costs are learned between them).  Every chain
+    still equals the oracle."""
     graphs = [rfmf.torus(30, 30, signed=True, seed=4), rfmf.erdos_renyi(600, 0.05, signed=True, seed=5)]
-    phases, iters = [128, 16, 1], [120, 120, 120]
+    phases, iters = [128, 16, 1], [400, 400, 400]
     dgs = [rfmf.DeviceGraph(ctx, g) for g in graphs]
     gl, ini, sol, t0, per = [], [], [], [], []
     for k, g in enumerate(graphs):
@@ -123,7 +123,7 @@ def test_items_resized_per_phase_keep_results(rfmf, ctx, oracle):
     b = rfmf.Batch(ctx, gl, t0, sol, ini, phases, iters)
     assert b.info()["launch_classes"] == 1
     for _ in range(4):
-        b.run_timed(90)
+        b.run_timed(300)
     info = b.info()
     r = b.read()
     b.close()
