@@ -310,7 +310,7 @@ typedef struct rfmf_batch_plan {
                                   3 8-byte, 4 16-bit, 5 32-bit entries */
     int gain_width;            /* bytes per vertex gain: 1 or 4 */
     int smem_bytes;            /* dynamic shared memory per CTA */
-    int balanced;              /* 1 once every multi-graph launch class sizes its work items from learned graph costs */
+    int balanced;              /* 1 once every multi-graph launch class sizes its work items per graph (from learned costs, else a shape model) */
     int launch_classes;        /* launches per window (graphs grouped by kernel variant and size) */
 } rfmf_batch_plan;
 

@@ -49,7 +49,7 @@ struct BatchClass {
     std::vector<int> Kg;                          // per class graph: chains per item
     std::vector<DevItem> items;
     std::vector<int32_t> order;
-    bool balanced = false;       // items sized from learned graph costs
+    bool balanced = false;       // items sized from graph costs (learned or modelled)
     uint64_t pendingSweeps = 0;  // sweeps of the last launch, whose item times are unread
     uint32_t pendingP = 0;       // its phase P (0: it spanned several phases)
     DevBuf dItems, dOrder, dItemNs, dCtl;
@@ -193,10 +193,10 @@ int plan_class(rfmf_batch& b, BatchClass& k, const rfmf_launch_config& c, bool e
 // Per-graph chains per item within a class, for phases of group count P.
 // An item's time per sweep depends on its graph and its scheduler level
 // (sched_level), so each graph's candidates are the largest chain count of
-// each level up to the class's K.  With learned costs for every graph, the
-// smallest makespan tau whose items all fit the resident CTA slots wins,
-// each graph taking its largest candidate with cost <= tau.  False (kg
-// untouched) when some graph has no cost yet or nothing fits.
+// each level up to the class's K.  With the graphs' costs (learned, else
+// the shape model), the smallest makespan tau whose items all fit the
+// resident CTA slots wins, each graph taking its largest candidate with
+// cost <= tau.  False (kg untouched) when nothing fits.
 bool plan_balanced(const rfmf_batch& b, const BatchClass& k, uint32_t P, std::vector<int>& kg) {
     const size_t G = k.graphs.size();
     if (G < 2) return false;
@@ -207,8 +207,9 @@ bool plan_balanced(const rfmf_batch& b, const BatchClass& k, uint32_t P, std::ve
         const rfmf_graph* g = b.glist[k.graphs[q]];
         for (int K = 1; K <= k.K; ++K) {
             if (K < k.K && sched_level(K + 1, k.warps) == sched_level(K, k.warps)) continue;
-            const double c = g->cost(k.warps, k.fmt, P, sched_level(K, k.warps));
-            if (c <= 0.0) return false;
+            const int L = sched_level(K, k.warps);
+            double c = g->cost(k.warps, k.fmt, P, L);
+            if (c <= 0.0) c = g->model_cost(k.warps, P, L);
             cand[q].push_back({K, c});
             taus.push_back(c);
         }
@@ -246,8 +247,9 @@ void build_items(const rfmf_batch& b, BatchClass& k, uint32_t P) {
     for (size_t q = 0; q < G; ++q) gorder[q] = static_cast<int>(q);
     auto itemCost = [&](int q) {
         const rfmf_graph* g = b.glist[k.graphs[q]];
-        const double learned = g->cost(k.warps, k.fmt, P, sched_level(k.Kg[q], k.warps));
-        return learned > 0.0 ? learned : static_cast<double>(g->n) * k.Kg[q];
+        const int L = sched_level(k.Kg[q], k.warps);
+        const double learned = g->cost(k.warps, k.fmt, P, L);
+        return learned > 0.0 ? learned : g->model_cost(k.warps, P, L);
     };
     std::stable_sort(gorder.begin(), gorder.end(), [&](int a, int z) { return itemCost(a) > itemCost(z); });
     k.items.clear();

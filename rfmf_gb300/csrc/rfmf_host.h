@@ -356,6 +356,19 @@ struct rfmf_graph {
         }
         return ns * (level + 3.0) / (bestL + 3.0);
     }
+    // Before any timing: an estimate of the same quantity from the graph's
+    // shape, fitted on GB300 to one-warp chains at 16 per SM (50x60 torus
+    // and ER n = 2000 d = 19, phases 128..1): 1.65 us + 1.03 ns per vertex +
+    // 3.5 ns per winner-row entry (min(P, n) rows of mean degree 2m/n), the
+    // vertex and entry terms spread over the chain's warps, scaled by level
+    // as above.  Within 7% of the measured sweep on both graphs at every P.
+    double model_cost(int warps, uint32_t P, int level) const {
+        const double nn = static_cast<double>(n > 0 ? n : 1);
+        const double rows = std::min(static_cast<double>(P > 0 ? P : 1), nn);
+        const double us = 1.65 + (1.03e-3 * nn + 3.5e-3 * rows * (2.0 * static_cast<double>(m) / nn)) /
+                                     static_cast<double>(warps > 0 ? warps : 1);
+        return 1e3 * us * (level + 3.0) / 7.0;
+    }
     void learn(int warps, int fmt, uint32_t P, int level, double ns, double weight) const {
         LearnedCost& c = costs[{warps, fmt, P > 0 ? P : 1u, level}];
         c.ns = (c.ns * c.weight + ns * weight) / (c.weight + weight);
