@@ -143,6 +143,11 @@ struct rfmf_server {
     std::thread worker;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // Launch classes of one window run side by side: one stream and one
+    // completion event per class, forked from and joined back to `stream`.
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaStream_t> clsStreams;
+    std::vector<cudaEvent_t> clsDone;
     std::vector<ReqPtr> running;
     SlotRanges slots;
     DevBuf dChains, dGraphs, dScheds, dItems, dOrder, dCtl;
@@ -345,12 +350,16 @@ int harvest(rfmf_server* s, Request& r) {
     return RFMF_OK;
 }
 
-// One window over the running requests: one launch per launch class.
+// One window over the running requests: one launch per launch class, the
+// classes side by side on their own streams (a class that fills only part
+// of the GPU no longer leaves the rest idle while the next one waits).
+// Each class has its own work items, item order and queue/error words.
 int run_window(rfmf_server* s, int64_t& launches, float& ms) {
     std::map<ClassKey, std::vector<Request*>> classes;
     for (const ReqPtr& r : s->running) classes[ClassKey{r->dbytes, r->fmt, r->W, r->s64}].push_back(r.get());
     launches = 0;
     ms = 0.0f;
+    const int ncls = static_cast<int>(classes.size());
     int64_t need = 0;
     for (const ReqPtr& r : s->running) need += r->C;
     if (need > s->itemCap) {
@@ -361,8 +370,35 @@ int run_window(rfmf_server* s, int64_t& launches, float& ms) {
             return rc;
         s->itemCap = cap;
     }
-    CU(cudaMemsetAsync(s->dCtl.p, 0, 16, s->stream));
-    CU(cudaEventRecord(s->ev0, s->stream));
+    if (s->dCtl.bytes < static_cast<size_t>(16) * ncls) {
+        DevBuf nb;
+        if (int rc = nb.alloc(static_cast<size_t>(16) * grow_to(ncls, ncls))) return rc;
+        std::swap(s->dCtl.p, nb.p);
+        std::swap(s->dCtl.bytes, nb.bytes);
+    }
+    while (static_cast<int>(s->clsStreams.size()) < ncls) {
+        cudaStream_t st = nullptr;
+        cudaEvent_t ev = nullptr;
+        CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+            cudaStreamDestroy(st);
+            return fail(RFMF_ERR_CUDA, "event creation failed");
+        }
+        s->clsStreams.push_back(st);
+        s->clsDone.push_back(ev);
+    }
+
+    // Plan every class on the host; their items and orders go up together.
+    struct Plan {
+        ClassKey k;
+        DevLaunch L;
+        int grid, threads;
+        size_t smem;
+    };
+    std::vector<Plan> plans;
+    std::vector<DevItem> items;
+    std::vector<int32_t> order;
+    int ci = 0;
     for (auto& kv : classes) {
         const ClassKey& k = kv.first;
         std::vector<Request*>& reqs = kv.second;
@@ -410,28 +446,24 @@ int run_window(rfmf_server* s, int64_t& launches, float& ms) {
         };
         int K = 1;
         while (K < Kshape && items_for(K) > slotsRes) ++K;
-        std::vector<DevItem> items;
-        std::vector<int32_t> order;
+        const size_t item0 = items.size(), order0 = order.size();
         for (auto& g : byGraph) {
             const std::vector<int32_t>& ch = g.second;
             for (size_t i = 0; i < ch.size(); i += K) {
                 const int cnt = static_cast<int>(std::min<size_t>(K, ch.size() - i));
-                items.push_back(DevItem{g.first, static_cast<int32_t>(order.size()), cnt, 0});
+                items.push_back(DevItem{g.first, static_cast<int32_t>(order.size() - order0), cnt, 0});
                 for (int q = 0; q < cnt; ++q) order.push_back(ch[i + q]);
             }
         }
-        CU(cudaMemcpyAsync(s->dItems.p, items.data(), items.size() * sizeof(DevItem),
-                           cudaMemcpyHostToDevice, s->stream));
-        CU(cudaMemcpyAsync(s->dOrder.p, order.data(), order.size() * sizeof(int32_t),
-                           cudaMemcpyHostToDevice, s->stream));
-        CU(cudaMemsetAsync(s->dCtl.p, 0, sizeof(int32_t), s->stream));   // queue head
-        DevLaunch L{};
+        Plan pl{};
+        pl.k = k;
+        DevLaunch& L = pl.L;
         L.graphs = s->dGraphs.as<DevGraph>();
         L.scheds = s->dScheds.as<DevSchedule>();
         L.chains = s->dChains.as<DevChain>();
-        L.items = s->dItems.as<DevItem>();
-        L.order = s->dOrder.as<int32_t>();
-        L.nitems = static_cast<int32_t>(items.size());
+        L.items = s->dItems.as<DevItem>() + item0;
+        L.order = s->dOrder.as<int32_t>() + order0;
+        L.nitems = static_cast<int32_t>(items.size() - item0);
         L.ngraphs = s->graphSlots;
         L.nscheds = s->schedSlots;
         L.warpsPerChain = k.W;
@@ -441,24 +473,46 @@ int run_window(rfmf_server* s, int64_t& launches, float& ms) {
         L.pmax = pmax;
         L.csrBytes = csrB;
         L.chainBytes = chainB;
-        L.queue = s->dCtl.as<int32_t>();
-        L.error = s->dCtl.as<int32_t>() + 1;
-        L.errorItem = s->dCtl.as<int32_t>() + 2;
+        L.queue = s->dCtl.as<int32_t>() + 4 * ci;
+        L.error = L.queue + 1;
+        L.errorItem = L.queue + 2;
         L.itemNs = nullptr;
         L.window = s->window;
         std::memcpy(L.lut, s->ctx->lut, sizeof L.lut);
-        const int grid = static_cast<int>(std::min<int64_t>(static_cast<int64_t>(items.size()), slotsRes));
-        const size_t smem = kSmemHeader + csrB + static_cast<size_t>(Kshape) * chainB;
-        CU(launch_anneal(L, k.dbytes, k.fmt, k.s64, grid, 32 * k.W * Kshape, smem, s->stream));
+        pl.grid = static_cast<int>(std::min<int64_t>(L.nitems, slotsRes));
+        pl.threads = 32 * k.W * Kshape;
+        pl.smem = kSmemHeader + csrB + static_cast<size_t>(Kshape) * chainB;
+        plans.push_back(pl);
+        ++ci;
+    }
+    CU(cudaMemcpyAsync(s->dItems.p, items.data(), items.size() * sizeof(DevItem), cudaMemcpyHostToDevice,
+                       s->stream));
+    CU(cudaMemcpyAsync(s->dOrder.p, order.data(), order.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                       s->stream));
+    CU(cudaMemsetAsync(s->dCtl.p, 0, static_cast<size_t>(16) * ncls, s->stream));
+    CU(cudaEventRecord(s->ev0, s->stream));
+    const bool fork = ncls > 1;
+    if (fork) CU(cudaEventRecord(s->fork, s->stream));
+    for (int c = 0; c < ncls; ++c) {
+        const Plan& pl = plans[c];
+        cudaStream_t st = fork ? s->clsStreams[c] : s->stream;
+        if (fork) CU(cudaStreamWaitEvent(st, s->fork, 0));
+        CU(launch_anneal(pl.L, pl.k.dbytes, pl.k.fmt, pl.k.s64, pl.grid, pl.threads, pl.smem, st));
+        if (fork) {
+            CU(cudaEventRecord(s->clsDone[c], st));
+            CU(cudaStreamWaitEvent(s->stream, s->clsDone[c], 0));
+        }
         ++launches;
     }
     CU(cudaEventRecord(s->ev1, s->stream));
-    int32_t ctl[4] = {0, 0, 0, 0};
-    CU(cudaMemcpyAsync(ctl, s->dCtl.p, sizeof ctl, cudaMemcpyDeviceToHost, s->stream));
+    std::vector<int32_t> ctl(static_cast<size_t>(4) * std::max(ncls, 1), 0);
+    CU(cudaMemcpyAsync(ctl.data(), s->dCtl.p, static_cast<size_t>(16) * ncls, cudaMemcpyDeviceToHost, s->stream));
     CU(cudaStreamSynchronize(s->stream));
     CU(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
-    if (ctl[1] != 0)
-        return fail(RFMF_ERR_CUDA, "device error %d in a server window (item %d)", ctl[1], ctl[2]);
+    for (int c = 0; c < ncls; ++c)
+        if (ctl[4 * c + 1] != 0)
+            return fail(RFMF_ERR_CUDA, "device error %d in a server window (item %d)", ctl[4 * c + 1],
+                        ctl[4 * c + 2]);
     return RFMF_OK;
 }
 
@@ -660,6 +714,7 @@ static int rfmf_server_create_impl(rfmf_context* ctx, const rfmf_server_config* 
     CU(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     CU(cudaEventCreate(&s->ev0));
     CU(cudaEventCreate(&s->ev1));
+    CU(cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming));
     if (int rc = s->dCtl.alloc(16)) return rc;
     s->t0 = Clock::now();
     rfmf_server* raw = s.get();
@@ -685,6 +740,9 @@ extern "C" int rfmf_server_destroy(rfmf_server* s) {
     s->queue.clear();
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->fork) cudaEventDestroy(s->fork);
+    for (cudaEvent_t e : s->clsDone) cudaEventDestroy(e);
+    for (cudaStream_t st : s->clsStreams) cudaStreamDestroy(st);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return RFMF_OK;
