@@ -325,18 +325,20 @@ uint32_t phase_at(const rfmf_batch& b, uint64_t sweep, uint64_t* end) {
 // from the costs learned so far (re-planned before every launch: costs
 // keep arriving, and planning is a few microseconds per graph); uploaded
 // only when the per-graph item sizes change (stream-ordered after older
-// launches).  A class without costs for every graph keeps its items.
-int rebalance(rfmf_batch* b, uint32_t P) {
+// launches).  *changed (optional) tells whether any class's items did.
+int rebalance(rfmf_batch* b, uint32_t P, bool* changed = nullptr) {
+    if (changed) *changed = false;
     for (BatchClass& k : b->cls) {
         if (k.graphs.size() < 2) continue;
         std::vector<int> kg;
         if (!plan_balanced(*b, k, P, kg)) continue;
-        const bool changed = !k.balanced || kg != k.Kg;
+        const bool differ = !k.balanced || kg != k.Kg;
         k.Kg = kg;
         k.balanced = true;
-        if (changed) {
+        if (differ) {
             build_items(*b, k, P);
             if (int rc = upload_items(*b, k)) return rc;
+            if (changed) *changed = true;
         }
     }
     return RFMF_OK;
@@ -829,15 +831,15 @@ static int rfmf_batch_run_impl(rfmf_batch* b, uint64_t sweeps) {
     return enqueue_run(b, sweeps);
 }
 
+// Captures `launches` windows of `sweeps` sweeps as one CUDA graph and
+// replays it.  Work items are sized for the phase the batch is in before
+// each replay; when that changes them (a new phase), the graph is captured
+// again (the launches' item counts are part of it).
 static int rfmf_batch_run_graph_impl(rfmf_batch* b, uint64_t sweeps, int launches, int replays) {
     if (!b || launches <= 0 || replays < 0) return fail(RFMF_ERR_INVALID, "bad arguments");
     CU(cudaSetDevice(b->ctx->device));
-    if (!b->graphExec || b->graphSweeps != sweeps || b->graphLaunches != launches) {
+    auto capture = [&]() -> int {
         if (b->graphExec) { cudaGraphExecDestroy(b->graphExec); b->graphExec = nullptr; }
-        // Items are sized before the capture, for the phase the batch is in
-        // (the graph replays them as they are).
-        uint64_t end = 0;
-        if (int rc = rebalance(b, phase_at(*b, b->hostDone, &end))) return rc;
         cudaGraph_t graph = nullptr;
         CU(cudaStreamBeginCapture(b->ctx->stream, cudaStreamCaptureModeThreadLocal));
         int rc = RFMF_OK;
@@ -850,8 +852,22 @@ static int rfmf_batch_run_graph_impl(rfmf_batch* b, uint64_t sweeps, int launche
         if (ei != cudaSuccess) { b->graphExec = nullptr; return fail(RFMF_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(ei)); }
         b->graphSweeps = sweeps;
         b->graphLaunches = launches;
-    }
+        return RFMF_OK;
+    };
+    auto sized = [&](bool& changed) {
+        uint64_t end = 0;
+        return rebalance(b, phase_at(*b, b->hostDone, &end), &changed);
+    };
+    bool changed = false;
+    if (int rc = sized(changed)) return rc;
+    if (!b->graphExec || b->graphSweeps != sweeps || b->graphLaunches != launches || changed)
+        if (int rc = capture()) return rc;
     for (int r = 0; r < replays; ++r) {
+        if (r > 0) {
+            if (int rc = sized(changed)) return rc;
+            if (changed)
+                if (int rc = capture()) return rc;
+        }
         CU(cudaGraphLaunch(b->graphExec, b->ctx->stream));
         for (int i = 0; i < launches; ++i)
             b->hostDone += std::min<uint64_t>(sweeps, b->total - std::min(b->total, b->hostDone));
