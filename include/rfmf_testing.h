@@ -29,6 +29,16 @@ int rfmf_batch_debug_set_cut(rfmf_batch* b, int64_t chain, int64_t cut);
  * countdown <= 0 disarms it.  Process-wide. */
 int rfmf_debug_fail_host_alloc(int64_t countdown);
 
+/* The batch planner's work-item sizing on given costs (no device work):
+ * `ngraphs` graphs of one launch class with chains[q] chains each, CTAs of
+ * at most `max_chains_per_cta` chains of `warps` warps, `slots` resident
+ * CTAs, and level_ns[q * L + l - 1] the time per sweep of an item of graph q
+ * at scheduler level l (warps on one SM scheduler, ceil(chains * warps / 4);
+ * L = the level of a full CTA).  out_chains_per_item[q] receives graph q's
+ * item size.  RFMF_ERR_CAPACITY when no sizes fit the slots. */
+int rfmf_debug_plan_items(int ngraphs, const int64_t* chains, int max_chains_per_cta, int warps,
+                          const double* level_ns, int64_t slots, int* out_chains_per_item);
+
 #ifdef __cplusplus
 }
 #endif

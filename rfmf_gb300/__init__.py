@@ -7,7 +7,8 @@ reference's interface in Python.  There is no CPU fallback.
 from ._lib import BatchPlan, LaunchConfig, RfmfError, lib
 from .api import (SOLVER_SEED_OFFSET, AnnealResult, Batch, Context, DeviceGraph, Server, anneal_gpu,
                   autotune,
-                  beta_fixed, beta_tables, cut_value, debug_fail_host_alloc, initial_spins,
+                  beta_fixed, beta_tables, cut_value, debug_fail_host_alloc, debug_plan_items,
+                  initial_spins,
                   make_config,
                   max_weighted_degree, parse_gset, score_safe_int32, solver_seed, total_steps,
                   version)
@@ -18,7 +19,7 @@ from .graphs import (CsrGraph, csr_from_edges, erdos_renyi, erdos_renyi_degree, 
 __all__ = [
     "BatchPlan", "LaunchConfig", "RfmfError", "lib", "SOLVER_SEED_OFFSET", "AnnealResult", "Batch",
     "Context", "DeviceGraph", "Server", "anneal_gpu", "beta_fixed", "beta_tables", "cut_value",
-    "debug_fail_host_alloc", "autotune",
+    "debug_fail_host_alloc", "debug_plan_items", "autotune",
     "initial_spins", "make_config", "max_weighted_degree", "parse_gset", "score_safe_int32", "solver_seed",
     "total_steps", "version", "CsrGraph", "csr_from_edges", "erdos_renyi",
     "erdos_renyi_degree", "erdos_renyi_sparse", "planar_like", "random_tree", "read_gset", "torus",

@@ -49,6 +49,7 @@ SIGNATURES = [
     ("rfmf_batch_restore", ct.c_int, [_P, _I64, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P,
                                       _P, _P]),
     ("rfmf_debug_fail_host_alloc", ct.c_int, [_I64]),
+    ("rfmf_debug_plan_items", ct.c_int, [ct.c_int, _P, ct.c_int, ct.c_int, _P, _I64, _P]),
     ("rfmf_batch_info", ct.c_int, [_P, _P]),
     ("rfmf_autotune", ct.c_int, [_P, _I64, _P, _P, _P, _P, _I64, _P, _P, _U64, _P, _P, _P, _P,
                                  _P]),

@@ -281,6 +281,20 @@ def debug_fail_host_alloc(countdown):
     check(lib().rfmf_debug_fail_host_alloc(int(countdown)))
 
 
+def debug_plan_items(chains, max_chains_per_cta, warps, level_ns, slots):
+    """Testing aid: the batch planner's item sizes for one launch class on
+    given costs (rfmf_debug_plan_items).  chains[q]: graph q's chains;
+    level_ns[q][l - 1]: its item time per sweep at scheduler level l.
+    Returns the chains per item of each graph."""
+    G = len(chains)
+    ch = np.ascontiguousarray(chains, np.int64)
+    ns = np.ascontiguousarray(level_ns, np.float64).reshape(G, -1)
+    out = np.zeros(G, np.int32)
+    check(lib().rfmf_debug_plan_items(G, _p(ch), int(max_chains_per_cta), int(warps), _p(ns),
+                                      int(slots), _p(out)))
+    return [int(x) for x in out]
+
+
 class Batch:
     """Chains over many graphs with device-resident state (rfmf_batch)."""
 

@@ -190,41 +190,31 @@ int plan_class(rfmf_batch& b, BatchClass& k, const rfmf_launch_config& c, bool e
     return RFMF_OK;
 }
 
-// Per-graph chains per item within a class, for phases of group count P.
-// An item's time per sweep depends on its graph and its scheduler level
-// (sched_level), so each graph's candidates are the largest chain count of
-// each level up to the class's K.  With the graphs' costs (learned, else
-// the shape model), the smallest makespan tau whose items all fit the
-// resident CTA slots wins, each graph taking its largest candidate with
-// cost <= tau.  False (kg untouched) when nothing fits.
-bool plan_balanced(const rfmf_batch& b, const BatchClass& k, uint32_t P, std::vector<int>& kg) {
-    const size_t G = k.graphs.size();
-    if (G < 2) return false;
-    struct Cand { int K; double ns; };
-    std::vector<std::vector<Cand>> cand(G);
+// Per-graph chains per item: graph q may use item sizes cand[q] (chain
+// count, item time per sweep; time non-decreasing in chain count), and all
+// items must fit `slots` resident CTAs.  The smallest makespan tau wins, each
+// graph taking its largest size whose time is <= tau.  False (kg untouched)
+// when nothing fits.
+struct ItemCand {
+    int K;
+    double ns;
+};
+bool balance_items(const std::vector<std::vector<ItemCand>>& cand, const std::vector<int64_t>& chains,
+                   int64_t slots, std::vector<int>& kg) {
+    const size_t G = cand.size();
     std::vector<double> taus;
-    for (size_t q = 0; q < G; ++q) {
-        const rfmf_graph* g = b.glist[k.graphs[q]];
-        for (int K = 1; K <= k.K; ++K) {
-            if (K < k.K && sched_level(K + 1, k.warps) == sched_level(K, k.warps)) continue;
-            const int L = sched_level(K, k.warps);
-            double c = g->cost(k.warps, k.fmt, P, L);
-            if (c <= 0.0) c = g->model_cost(k.warps, P, L);
-            cand[q].push_back({K, c});
-            taus.push_back(c);
-        }
-    }
-    const int64_t slots = static_cast<int64_t>(k.occ) * b.ctx->sms;
+    for (const auto& cq : cand)
+        for (const ItemCand& c : cq) taus.push_back(c.ns);
     std::sort(taus.begin(), taus.end());
     auto pick = [&](double tau, std::vector<int>& out) {
         int64_t items = 0;
         for (size_t q = 0; q < G; ++q) {
             int K = 0;
-            for (const Cand& c : cand[q])
+            for (const ItemCand& c : cand[q])
                 if (c.ns <= tau) K = c.K;
             if (!K) return false;
             out[q] = K;
-            items += (static_cast<int64_t>(k.chainsOf[q].size()) + K - 1) / K;
+            items += (chains[q] + K - 1) / K;
         }
         return items <= slots;
     };
@@ -237,6 +227,30 @@ bool plan_balanced(const rfmf_batch& b, const BatchClass& k, uint32_t P, std::ve
     if (lo == taus.size() || !pick(taus[lo], trial)) return false;
     kg = trial;
     return true;
+}
+
+// Per-graph chains per item within a class, for phases of group count P.
+// An item's time per sweep depends on its graph and its scheduler level
+// (sched_level), so each graph's candidates are the largest chain count of
+// each level up to the class's K, timed by the graph's costs (learned, else
+// the shape model).
+bool plan_balanced(const rfmf_batch& b, const BatchClass& k, uint32_t P, std::vector<int>& kg) {
+    const size_t G = k.graphs.size();
+    if (G < 2) return false;
+    std::vector<std::vector<ItemCand>> cand(G);
+    std::vector<int64_t> chains(G);
+    for (size_t q = 0; q < G; ++q) {
+        const rfmf_graph* g = b.glist[k.graphs[q]];
+        chains[q] = static_cast<int64_t>(k.chainsOf[q].size());
+        for (int K = 1; K <= k.K; ++K) {
+            if (K < k.K && sched_level(K + 1, k.warps) == sched_level(K, k.warps)) continue;
+            const int L = sched_level(K, k.warps);
+            double c = g->cost(k.warps, k.fmt, P, L);
+            if (c <= 0.0) c = g->model_cost(k.warps, P, L);
+            cand[q].push_back({K, c});
+        }
+    }
+    return balance_items(cand, chains, static_cast<int64_t>(k.occ) * b.ctx->sms, kg);
 }
 
 // Items: graphs in decreasing per-item cost, each graph's chains in groups of
@@ -1320,6 +1334,29 @@ extern "C" int rfmf_batch_stats(rfmf_batch* b, uint64_t* improved_sweeps) {
         return rfmf::fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_batch_stats");
     } catch (...) {
         return rfmf::fail(RFMF_ERR_INVALID, "unexpected host exception in rfmf_batch_stats");
+    }
+}
+
+extern "C" int rfmf_debug_plan_items(int ngraphs, const int64_t* chains, int max_chains_per_cta,
+                                     int warps, const double* level_ns, int64_t slots, int* out_chains_per_item) {
+    if (ngraphs < 1 || !chains || max_chains_per_cta < 1 || warps < 1 || !level_ns || slots < 1 ||
+        !out_chains_per_item)
+        return fail(RFMF_ERR_INVALID, "bad arguments");
+    try {
+        const int levels = sched_level(max_chains_per_cta, warps);
+        std::vector<std::vector<ItemCand>> cand(static_cast<size_t>(ngraphs));
+        std::vector<int64_t> ch(chains, chains + ngraphs);
+        for (int q = 0; q < ngraphs; ++q)
+            for (int K = 1; K <= max_chains_per_cta; ++K) {
+                if (K < max_chains_per_cta && sched_level(K + 1, warps) == sched_level(K, warps)) continue;
+                cand[q].push_back({K, level_ns[static_cast<size_t>(q) * levels + sched_level(K, warps) - 1]});
+            }
+        std::vector<int> kg;
+        if (!balance_items(cand, ch, slots, kg)) return fail(RFMF_ERR_CAPACITY, "no item sizes fit %lld slots", (long long)slots);
+        std::copy(kg.begin(), kg.end(), out_chains_per_item);
+        return RFMF_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(RFMF_ERR_NOMEM, "host allocation failed in rfmf_debug_plan_items");
     }
 }
 
