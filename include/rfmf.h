@@ -437,9 +437,8 @@ int rfmf_cancel(rfmf_server* s, uint64_t request_id);
  * RFMF_ERR_INVALID before any device work.  Synchronous on `stream` (a
  * cudaStream_t, NULL for the legacy default stream): it returns once the
  * anneal has finished.  The first call on a device looks up the array's
- * address and should come before any stream capture; the array is shared by
- * all calls, which clear what they need, and calls that overlap on the GPU
- * race on it.
+ * address; the array is shared by all calls, which clear what they need,
+ * and calls that overlap on the GPU race on it.
  */
 int rfmf_anneal_noalloc(int device, void* stream, int64_t n, const uint32_t* d_offsets,
                         const int32_t* d_edges, int64_t max_weighted_deg, int64_t C,

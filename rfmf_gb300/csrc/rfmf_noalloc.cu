@@ -13,8 +13,8 @@
 // array that every GPU that loads this library holds until the process exits.
 //
 // Set-up: the first call on a device, with that device current, looks up
-// the array's device address (cudaGetSymbolAddress) and caches it; make that
-// first call before any stream capture.  The array is shared by every call
+// the array's device address (cudaGetSymbolAddress) and caches it.  The
+// array is shared by every call
 // and keeps the last call's contents; each call rewrites the records and
 // clears the queue head and error word before its launches.  Calls whose
 // launches overlap on the GPU (different streams, or different host threads
