@@ -14,9 +14,9 @@
 //
 // Set-up: the first call on a device, with that device current, looks up
 // the array's device address (cudaGetSymbolAddress) and caches it.  The
-// array is shared by every call
-// and keeps the last call's contents; each call rewrites the records and
-// clears the queue head and error word before its launches.  Calls whose
+// array is shared by every call and keeps the last call's contents; each
+// call rewrites the records and clears the queue head and error word before
+// its launches.  Calls whose
 // launches overlap on the GPU (different streams, or different host threads
 // on one device) race on the array: serialise them.
 //
