@@ -312,6 +312,8 @@ typedef struct rfmf_batch_plan {
     int smem_bytes;            /* dynamic shared memory per CTA */
     int balanced;              /* 1 once every multi-graph launch class sizes its work items per graph (from learned costs, else a shape model) */
     int launch_classes;        /* launches per window (graphs grouped by kernel variant and size) */
+    int64_t launches;          /* kernel launches enqueued so far (a window of a multi-graph class
+                                  is cut at phase boundaries; graph replays count theirs) */
 } rfmf_batch_plan;
 
 int rfmf_batch_info(const rfmf_batch* b, rfmf_batch_plan* out);

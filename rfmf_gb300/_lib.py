@@ -89,7 +89,7 @@ class BatchPlan(ct.Structure):
                 ("threads_per_chain", ct.c_int), ("chains_per_cta", ct.c_int),
                 ("grid", ct.c_int), ("items", ct.c_int), ("score64", ct.c_int),
                 ("csr_format", ct.c_int), ("gain_width", ct.c_int), ("smem_bytes", ct.c_int),
-                ("balanced", ct.c_int), ("launch_classes", ct.c_int)]
+                ("balanced", ct.c_int), ("launch_classes", ct.c_int), ("launches", ct.c_int64)]
 
 
 class ServerConfig(ct.Structure):

@@ -80,6 +80,7 @@ struct rfmf_batch {
     cudaGraphExec_t graphExec = nullptr;
     uint64_t graphSweeps = 0;
     int graphLaunches = 0;
+    int64_t launches = 0;        // kernel launches enqueued (captured ones when replayed)
     ~rfmf_batch() {
         if (graphExec) cudaGraphExecDestroy(graphExec);
         for (BatchClass& k : cls) {
@@ -386,6 +387,7 @@ int launch_window(rfmf_batch* b, uint64_t sweeps) {
 // the cut (a chain's sweeps are a function of its sweep index alone).
 int enqueue_run(rfmf_batch* b, uint64_t sweeps, bool capturing = false) {
     if (capturing) return launch_window(b, sweeps);
+    const int64_t perWindow = static_cast<int64_t>(b->cls.size());
     uint64_t left = std::min<uint64_t>(sweeps, b->total - std::min(b->total, b->hostDone));
     bool split = false;
     for (const BatchClass& k : b->cls) split = split || k.graphs.size() > 1;
@@ -399,6 +401,7 @@ int enqueue_run(rfmf_batch* b, uint64_t sweeps, bool capturing = false) {
             k.pendingSweeps = left;
             k.pendingP = onePhase ? P0 : 0;
         }
+        b->launches += perWindow;
         return launch_window(b, sweeps);
     }
     while (left) {
@@ -411,6 +414,7 @@ int enqueue_run(rfmf_batch* b, uint64_t sweeps, bool capturing = false) {
             k.pendingSweeps = piece;
             k.pendingP = P;
         }
+        b->launches += perWindow;
         if (int rc = launch_window(b, piece)) return rc;
     }
     return RFMF_OK;
@@ -883,6 +887,7 @@ static int rfmf_batch_run_graph_impl(rfmf_batch* b, uint64_t sweeps, int launche
                 if (int rc = capture()) return rc;
         }
         CU(cudaGraphLaunch(b->graphExec, b->ctx->stream));
+        b->launches += static_cast<int64_t>(launches) * static_cast<int64_t>(b->cls.size());
         for (int i = 0; i < launches; ++i)
             b->hostDone += std::min<uint64_t>(sweeps, b->total - std::min(b->total, b->hostDone));
     }
@@ -1028,6 +1033,7 @@ extern "C" int rfmf_batch_info(const rfmf_batch* b, rfmf_batch_plan* out) {
     out->smem_bytes = static_cast<int>(big->smem);
     out->balanced = balanced ? 1 : 0;
     out->launch_classes = static_cast<int>(b->cls.size());
+    out->launches = b->launches;
     return RFMF_OK;
 }
 

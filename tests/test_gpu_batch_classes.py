@@ -128,6 +128,9 @@ def test_items_resized_per_phase_keep_results(rfmf, ctx, oracle):
     r = b.read()
     b.close()
     assert info["balanced"] == 1, info
+    # windows [0,300) [300,600) [600,900) [900,1200) over phases ending at
+    # 400, 800, 1200: cut into 1 + 2 + 2 + 1 launches of the one class
+    assert info["launches"] == 6, info
     for k, g in enumerate(graphs):
         init, solver, ts = per[k]
         ref = oracle.anneal(g, init, ts, solver, phases, iters)
