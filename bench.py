@@ -9,11 +9,14 @@ with mean degree ~19 (weights uniform +-1), 1024 chains per graph (raw seeds
 35,50,70,100,140,200,280,400 assigned round-robin.  Synthetic seeded graphs
 of those shapes stand in for the Gset instances.
 
-One STEP is one persistent launch that advances all 2048 chains by
-sweeps/steps sweeps; the K timed steps together are one complete anneal of
---sweeps sweeps per chain (default 10^7, the configuration's budget), with the
-chain state resident on the device between steps.  value = chains * sweeps /
-(sum of the K launch times, CUDA events on the library's stream).  The L2 is
+One STEP is one rfmf_batch_run_timed window that advances all 2048 chains by
+sweeps/steps sweeps (one persistent launch, or one per phase where the
+window crosses a phase boundary: both graphs share a launch class, whose
+work items are sized per phase); the K timed steps together are one
+complete anneal of --sweeps sweeps per chain (default 10^7, the
+configuration's budget), with the chain state resident on the device
+between steps.  value = chains * sweeps / (sum of the K window times, CUDA
+events on the library's stream).  The L2 is
 flushed (256 MB write) between timed steps, outside the events.
 
 e2e: the same metric through the public drop-in call (rfmf_graph_create +
@@ -517,7 +520,7 @@ def plain_kernel_arm(graphs, setup, sweeps, ctx):
     state in global memory), compiled from its sources for sm_103a and
     launched through oracle/refgpu.py, on a bounded sample of the same
     workload; against librfmf.so on the identical sample in two forms: the
-    batched form (both graphs' chains in one batch, one persistent launch)
+    batched form (both graphs' chains in one batch, one launch per phase)
     and the annealGpu drop-in (one rfmf_anneal call per graph).  All three
     must give identical results chain for chain."""
     sys.path.insert(0, str(ROOT / "oracle"))
@@ -582,7 +585,7 @@ def plain_kernel_arm(graphs, setup, sweeps, ctx):
                       f"(phases 128..1); reference threads/block {tpbs}",
             "identical_results": True,
             "what": "reference mcKernel (its sources built for sm_103a), one launch per graph, "
-                    "kernel-only cudaEvent time; ours: both graphs in one batch (one launch), and "
+                    "kernel-only cudaEvent time; ours: both graphs in one batch (one launch per phase), and "
                     "rfmf_anneal per graph"}
 
 
