@@ -157,3 +157,42 @@ def test_few_chains_of_a_large_graph_get_eight_warps(rfmf, ctx):
         b.close()
         dg.close()
     assert widths == {"torus": 256, "er": 128}, widths
+
+
+def test_phase_cuts_with_skipped_and_oversized_phases(rfmf, ctx, oracle):
+    """Phase cuts over a schedule with P = 0 phases (skipped, sweep ids not
+    advanced) and a P larger than n (the kernel clamps it): a two-graph
+    class run in windows that straddle every boundary still equals the
+    oracle, chain for chain."""
+    graphs = [rfmf.erdos_renyi(240, 0.05, signed=True, seed=21),
+              rfmf.torus(12, 20, signed=True, seed=22)]
+    phases, iters = [0, 5000, 0, 3, 1], [70, 130, 50, 110, 90]
+    dgs = [rfmf.DeviceGraph(ctx, g) for g in graphs]
+    gl, ini, sol, t0, per = [], [], [], [], []
+    for k, g in enumerate(graphs):
+        init, solver = chains_for(g, list(range(40 * k, 40 * k + 24)))
+        ts = [40.0 + 20 * (i % 6) for i in range(24)]
+        per.append((init, solver, ts))
+        gl += [dgs[k]] * 24
+        ini += list(init)
+        sol += solver
+        t0 += ts
+    b = rfmf.Batch(ctx, gl, t0, sol, ini, phases, iters)
+    assert b.info()["launch_classes"] == 1
+    for w in (57, 100, 1000):
+        b.run(w)
+    r = b.read()
+    info = b.info()
+    b.close()
+    # executed sweeps: 130 (P = 5000) then 110 (P = 3) then 90 (P = 1);
+    # windows [0,57) [57,157) [157,330): 1 + 2 + 2 launches
+    assert info["launches"] == 5, info
+    for k, g in enumerate(graphs):
+        init, solver, ts = per[k]
+        ref = oracle.anneal(g, init, ts, solver, phases, iters)
+        sl = slice(24 * k, 24 * k + 24)
+        assert np.array_equal(np.stack(r["end_spins"][sl]), ref["end_spins"]), k
+        assert np.array_equal(np.stack(r["best_spins"][sl]), ref["best_spins"]), k
+        assert np.array_equal(r["best_vals"][sl], ref["best_vals"]), k
+    for dg in dgs:
+        dg.close()
