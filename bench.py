@@ -860,6 +860,7 @@ def serving_arm(args, ctx, rate, budgets=None, max_requests=None, compare_offlin
     srv = R.Server(ctx, window_sweeps=args.serve_window)
     ids = [None] * len(reqs)
     err = []
+    submit_s = []     # duration of each Server.submit call (rfmf_submit + Python marshalling)
 
     # Request inputs are built before the arrival stream starts, so that the
     # submitting thread only calls submit (building initial spins in the loop
@@ -881,7 +882,9 @@ def serving_arm(args, ctx, rate, budgets=None, max_requests=None, compare_offlin
                 time.sleep(d)
             try:
                 phases, iters = schedule(r["sweeps"])
+                ts = time.perf_counter()
                 ids[i] = srv.submit(dgs[r["g"]], init, t0s, phases, iters, solver)
+                submit_s.append(time.perf_counter() - ts)
                 submitted[i] = time.perf_counter() - t0
             except Exception as e:   # pragma: no cover
                 err.append(repr(e))
@@ -932,6 +935,8 @@ def serving_arm(args, ctx, rate, budgets=None, max_requests=None, compare_offlin
     return {"rate_req_s": rate, "requests": len(reqs),
             "arrival_window_s": arrivals[-1] if arrivals else 0.0,
             "offered_rate_req_s": (len(submitted) - 1) / span if span > 0 else None,
+            "submit_ms_p50": float(np.percentile(submit_s, 50) * 1e3) if submit_s else None,
+            "submit_ms_p99": float(np.percentile(submit_s, 99) * 1e3) if submit_s else None,
             "sweeps_per_request": sorted(set(r["sweeps"] for r in reqs)),
             "window_sweeps": args.serve_window,
             "latency_by_budget": {str(k): {"requests": len(v), "p50_s": float(np.percentile(v, 50)),
