@@ -13,8 +13,11 @@
 //     occupancy API, the smallest that keeps every work item resident) and
 //     runs as its own persistent launch; classes of one window go out on
 //     separate streams and share the GPU;
-//   * work items are resized from per-graph device costs learned from the
-//     item timings (%globaltimer) of earlier launches.
+//   * in a class of several graphs, each graph's chains per work item are
+//     sized per phase from item costs by scheduler level (learned from the
+//     %globaltimer item timings of earlier launches, else a shape model),
+//     and a window is cut at phase boundaries so each piece runs with the
+//     items of its phase.
 #include <cuda_runtime.h>
 
 #include <algorithm>
