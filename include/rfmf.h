@@ -278,7 +278,7 @@ int rfmf_batch_restore(rfmf_context* ctx, int64_t nchains, const rfmf_graph* con
  * src/tuning.hpp:10-17, applied at src/anneal_kernels.cu:641-662).  Times
  * candidate plans on short trial batches of these very chains (their graphs,
  * seeds, t0s and initial spins; the schedule compressed to trial_sweeps
- * sweeps with every phase keeping its share, 0 = 512) and writes the fastest
+ * sweeps with every phase keeping its share, 0 = 2048) and writes the fastest
  * to *best, starting from *base (NULL: all automatic).  Candidates: warps per
  * chain from the planner's rule or fixed at 1, 2 or 4, each with the rule's
  * CSR residency or with HBM walks.  Each candidate runs twice and keeps its

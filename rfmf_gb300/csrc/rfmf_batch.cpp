@@ -45,6 +45,7 @@ constexpr uint64_t kMinLearnSweeps = 256;
 struct BatchClass {
     bool score64 = false;
     int dbytes = 1, fmt = kCsrGlobal, warps = 1;
+    int baseWarps = 1;           // the planner's width; `warps` may double per phase
     int K = 1, threads = 32, grid = 0, occ = 1, nitems = 0, pmax = 1;
     size_t smem = 0;
     std::vector<int> graphs;                      // batch graph indices
@@ -84,6 +85,8 @@ struct rfmf_batch {
     uint64_t graphSweeps = 0;
     int graphLaunches = 0;
     int64_t launches = 0;        // kernel launches enqueued (captured ones when replayed)
+    rfmf_launch_config cfg{};    // the creation config (re-planning per phase)
+    bool phaseWarps = false;     // the one class's width follows the phase
     ~rfmf_batch() {
         if (graphExec) cudaGraphExecDestroy(graphExec);
         for (BatchClass& k : cls) {
@@ -233,25 +236,39 @@ bool balance_items(const std::vector<std::vector<ItemCand>>& cand, const std::ve
     return true;
 }
 
+// Whether every graph of class k has a cost learned at phase P.
+bool class_learned(const rfmf_batch& b, const BatchClass& k, uint32_t P) {
+    bool learned = true;
+    for (int gi : k.graphs) learned = learned && b.glist[gi]->learned_at(k.warps, k.fmt, P);
+    return learned;
+}
+
+// An item's time per sweep for graph q of class k at level L: learned, or
+// modelled (for all graphs of the class alike).
+double item_cost(const rfmf_batch& b, const BatchClass& k, size_t q, uint32_t P, int L, bool learned) {
+    const rfmf_graph* g = b.glist[k.graphs[q]];
+    return learned ? g->cost(k.warps, k.fmt, P, L) : g->model_cost(k.warps, P, L);
+}
+
 // Per-graph chains per item within a class, for phases of group count P.
 // An item's time per sweep depends on its graph and its scheduler level
 // (sched_level), so each graph's candidates are the largest chain count of
-// each level up to the class's K, timed by the graph's costs (learned, else
-// the shape model).
+// each level up to the class's K, timed by the graphs' costs learned at P
+// when every graph has some, else all by the shape model (learned and
+// modelled costs are not on one scale: a cost learned in another batch
+// shape, extrapolated to this one's levels, beside a modelled one, misled
+// the split).
 bool plan_balanced(const rfmf_batch& b, const BatchClass& k, uint32_t P, std::vector<int>& kg) {
     const size_t G = k.graphs.size();
     if (G < 2) return false;
+    const bool learned = class_learned(b, k, P);
     std::vector<std::vector<ItemCand>> cand(G);
     std::vector<int64_t> chains(G);
     for (size_t q = 0; q < G; ++q) {
-        const rfmf_graph* g = b.glist[k.graphs[q]];
         chains[q] = static_cast<int64_t>(k.chainsOf[q].size());
         for (int K = 1; K <= k.K; ++K) {
             if (K < k.K && sched_level(K + 1, k.warps) == sched_level(K, k.warps)) continue;
-            const int L = sched_level(K, k.warps);
-            double c = g->cost(k.warps, k.fmt, P, L);
-            if (c <= 0.0) c = g->model_cost(k.warps, P, L);
-            cand[q].push_back({K, c});
+            cand[q].push_back({K, item_cost(b, k, q, P, sched_level(K, k.warps), learned)});
         }
     }
     return balance_items(cand, chains, static_cast<int64_t>(k.occ) * b.ctx->sms, kg);
@@ -263,11 +280,9 @@ void build_items(const rfmf_batch& b, BatchClass& k, uint32_t P) {
     const size_t G = k.graphs.size();
     std::vector<int> gorder(G);
     for (size_t q = 0; q < G; ++q) gorder[q] = static_cast<int>(q);
+    const bool learned = class_learned(b, k, P);
     auto itemCost = [&](int q) {
-        const rfmf_graph* g = b.glist[k.graphs[q]];
-        const int L = sched_level(k.Kg[q], k.warps);
-        const double learned = g->cost(k.warps, k.fmt, P, L);
-        return learned > 0.0 ? learned : g->model_cost(k.warps, P, L);
+        return item_cost(b, k, static_cast<size_t>(q), P, sched_level(k.Kg[q], k.warps), learned);
     };
     std::stable_sort(gorder.begin(), gorder.end(), [&](int a, int z) { return itemCost(a) > itemCost(z); });
     k.items.clear();
@@ -362,6 +377,58 @@ int rebalance(rfmf_batch* b, uint32_t P, bool* changed = nullptr) {
     return RFMF_OK;
 }
 
+// Warps per chain for phases of group count P in a batch whose width
+// follows the phase (one class, one graph, one-warp chains by rule, every
+// chain resident at two warps): two warps while the winners' rows hold at
+// least half as many entries as the graph has vertices (P >= 64), one
+// otherwise.  GB300, 1024 chains of ER n = 2000 d = 19, us per sweep at one
+// / two warps: P = 128 10.0 / 8.08, P = 64 6.11 / 5.43, P = 32 4.14 / 4.60,
+// P = 1 2.41 / 2.88; the 50x60 torus (512 row entries at P = 128) is
+// faster at one warp in every phase.
+bool wide_phase(const rfmf_graph* g, uint32_t P) {
+    const double n = static_cast<double>(g->n);
+    const double rows = std::min(static_cast<double>(P), n);
+    return P >= 64 && 2.0 * rows * (2.0 * static_cast<double>(g->m) / n) >= n;
+}
+
+int phase_warps(const rfmf_batch& b, const BatchClass& k, uint32_t P) {
+    if (!b.phaseWarps) return k.warps;
+    return wide_phase(b.glist[k.graphs[0]], P) ? 2 * k.baseWarps : k.baseWarps;
+}
+
+// Re-plans class k at `warps` per chain (CTA shape, items) for phase P.  A
+// width that does not plan keeps the current one.
+int set_warps(rfmf_batch* b, BatchClass& k, int warps, uint32_t P, bool* changed) {
+    const int old = k.warps;
+    k.warps = warps;
+    if (plan_class(*b, k, b->cfg, false) != RFMF_OK) {
+        k.warps = old;
+        return plan_class(*b, k, b->cfg, false);
+    }
+    build_items(*b, k, P);
+    if (int rc = upload_items(*b, k)) return rc;
+    if (changed) *changed = true;
+    return RFMF_OK;
+}
+
+// Everything that depends on the phase, before a launch in phase P: the
+// width of a batch whose width follows the phase, then the item sizes of
+// multi-graph classes.  *changed (optional) tells whether any launch shape
+// or item list changed.
+int prepare_phase(rfmf_batch* b, uint32_t P, bool* changed = nullptr) {
+    bool any = false;
+    if (b->phaseWarps) {
+        BatchClass& k = b->cls[0];
+        const int W = phase_warps(*b, k, P);
+        if (W != k.warps)
+            if (int rc = set_warps(b, k, W, P, &any)) return rc;
+    }
+    bool reb = false;
+    if (int rc = rebalance(b, P, &reb)) return rc;
+    if (changed) *changed = any || reb;
+    return RFMF_OK;
+}
+
 // One launch per class over `sweeps` sweeps.  A single class goes out on
 // the context's stream; several are forked onto their own streams and
 // joined back, so run_timed events and graph capture see the whole window.
@@ -392,12 +459,12 @@ int enqueue_run(rfmf_batch* b, uint64_t sweeps, bool capturing = false) {
     if (capturing) return launch_window(b, sweeps);
     const int64_t perWindow = static_cast<int64_t>(b->cls.size());
     uint64_t left = std::min<uint64_t>(sweeps, b->total - std::min(b->total, b->hostDone));
-    bool split = false;
+    bool split = b->phaseWarps;
     for (const BatchClass& k : b->cls) split = split || k.graphs.size() > 1;
     uint64_t end = 0;
     const uint32_t P0 = phase_at(*b, b->hostDone, &end);
     if (!split || left == 0 || left <= end - b->hostDone) {
-        if (int rc = rebalance(b, P0)) return rc;
+        if (int rc = prepare_phase(b, P0)) return rc;
         const bool onePhase = left > 0 && left <= end - b->hostDone;
         b->hostDone += left;
         for (BatchClass& k : b->cls) {
@@ -410,7 +477,7 @@ int enqueue_run(rfmf_batch* b, uint64_t sweeps, bool capturing = false) {
     while (left) {
         const uint32_t P = phase_at(*b, b->hostDone, &end);
         const uint64_t piece = std::min<uint64_t>(left, end - b->hostDone);
-        if (int rc = rebalance(b, P)) return rc;
+        if (int rc = prepare_phase(b, P)) return rc;
         b->hostDone += piece;
         left -= piece;
         for (BatchClass& k : b->cls) {
@@ -690,6 +757,13 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
         }
         if (rc) return rc;
     }
+    b->cfg = c;
+    for (BatchClass& k : b->cls) k.baseWarps = k.warps;
+    if (b->cls.size() == 1 && b->cls[0].graphs.size() == 1 && c.threads_per_chain == 0 && b->cls[0].warps == 1 &&
+        b->C * 2 <= int64_t(16) * ctx->sms) {
+        for (uint32_t P : b->phaseP)
+            b->phaseWarps = b->phaseWarps || (P && wide_phase(b->glist[b->cls[0].graphs[0]], P));
+    }
     {
         uint64_t end = 0;
         const uint32_t P0 = phase_at(*b, 0, &end);
@@ -877,7 +951,7 @@ static int rfmf_batch_run_graph_impl(rfmf_batch* b, uint64_t sweeps, int launche
     };
     auto sized = [&](bool& changed) {
         uint64_t end = 0;
-        return rebalance(b, phase_at(*b, b->hostDone, &end), &changed);
+        return prepare_phase(b, phase_at(*b, b->hostDone, &end), &changed);
     };
     bool changed = false;
     if (int rc = sized(changed)) return rc;
@@ -1149,7 +1223,7 @@ static int rfmf_autotune_impl(rfmf_context* ctx, int64_t C, const rfmf_graph* co
     if (!ctx || !best || !graphs || C <= 0 || nphases < 0 || (nphases > 0 && (!phases || !iters)))
         return fail(RFMF_ERR_INVALID, "bad arguments");
     const rfmf_launch_config b0 = base ? *base : rfmf_launch_config{};
-    const uint64_t trial = trial_sweeps ? trial_sweeps : 512;
+    const uint64_t trial = trial_sweeps ? trial_sweeps : 2048;
     const std::string key = tune_key(C, graphs, nphases, phases, iters, trial, b0);
     auto report = [&](const rfmf_context::TunedPlan& t) {
         *best = t.best;

@@ -369,6 +369,12 @@ struct rfmf_graph {
                                      static_cast<double>(warps > 0 ? warps : 1);
         return 1e3 * us * (level + 3.0) / 7.0;
     }
+    // Whether a cost was learned under the plan at phase P itself (any level).
+    bool learned_at(int warps, int fmt, uint32_t P) const {
+        auto it = costs.lower_bound({warps, fmt, P, 0});
+        return it != costs.end() && std::get<0>(it->first) == warps && std::get<1>(it->first) == fmt &&
+               std::get<2>(it->first) == P;
+    }
     void learn(int warps, int fmt, uint32_t P, int level, double ns, double weight) const {
         LearnedCost& c = costs[{warps, fmt, P > 0 ? P : 1u, level}];
         c.ns = (c.ns * c.weight + ns * weight) / (c.weight + weight);

@@ -196,3 +196,35 @@ def test_phase_cuts_with_skipped_and_oversized_phases(rfmf, ctx, oracle):
         assert np.array_equal(r["best_vals"][sl], ref["best_vals"]), k
     for dg in dgs:
         dg.close()
+
+
+def test_chain_width_follows_the_phase(rfmf, ctx, oracle):
+    """One dense graph with 700 chains (one warp per chain by rule; every
+    chain still resident at two): the P = 128 phase, whose winner rows hold
+    more entries than the graph has vertices, runs two warps per chain and
+    the later phases one; windows straddle the switches and every chain
+    equals the oracle."""
+    g = rfmf.erdos_renyi_degree(600, 19, signed=True, seed=8)
+    C = 700
+    init, solver = chains_for(g, list(range(3000, 3000 + C)))
+    t0s = [35.0 + 15 * (i % 8) for i in range(C)]
+    phases, iters = [128, 16, 1], [150, 150, 150]
+    dg = rfmf.DeviceGraph(ctx, g)
+    b = rfmf.Batch(ctx, [dg] * C, t0s, solver, list(init), phases, iters)
+    b.run_timed(100)
+    wide = b.info()["threads_per_chain"]
+    b.run_timed(100)
+    narrow = b.info()["threads_per_chain"]
+    b.run(1000)
+    info = b.info()
+    r = b.read()
+    b.close()
+    dg.close()
+    assert (wide, narrow) == (64, 32), (wide, narrow)
+    # [0,100) P=128; [100,150) P=128 + [150,200) P=16; [200,300) P=16 + [300,450) P=1
+    assert info["launches"] == 5, info
+    ref = oracle.anneal(g, init, t0s, solver, phases, iters)
+    assert np.array_equal(np.stack(r["end_spins"]), ref["end_spins"])
+    assert np.array_equal(np.stack(r["best_spins"]), ref["best_spins"])
+    assert np.array_equal(r["cur_vals"], ref["cur_vals"])
+    assert np.array_equal(r["best_vals"], ref["best_vals"])
