@@ -603,8 +603,20 @@ int choose_warps(int maxN, const rfmf_launch_config& c, int64_t chains, int sms)
     // alone fill the SMs; below that, per-chain latency is what the extra
     // warps buy (GB300, 256 chains of ER n = 2000: 67.5 -> 88.6 M
     // chain-steps/s from one warp to four; 32 chains of ER n = 800: 6.7 -> 11.0).
+    const int sized = W;
     while (W < kMaxAutoWarps && chains > 0 && chains * 2 * W <= int64_t(8) * sms && nblk >= 32 * W)
         W *= 2;
+    // Two warps for latency alone lose to one on graphs of under 4096
+    // vertices (16 vertex blocks per lane) outside the phases heavy in
+    // winner rows, which a one-graph batch widens by itself (GB300, 512
+    // chains, us per sweep at one / two warps: ER n = 2000 d = 19 P = 128
+    // 9.10 / 6.84 but P = 8 2.37 / 3.15 and P = 1 1.98 / 2.23; the 50x60
+    // torus 4.11 / 4.10 at P = 128, 2.44 / 3.20 at P = 8); on larger ones
+    // two win at every phase (ER n = 5000 d = 5 P = 1 3.57 / 3.15, P = 16
+    // 4.43 / 4.24; 70x70 torus and random tree n = 5000 alike); four, where
+    // the chains are few enough, win at every phase (256 chains: ER n = 2000
+    // 4.65 / 9.10 at P = 128 and 1.89 / 1.98 at P = 1 for four / one).
+    if (sized == 1 && W == 2 && nblk < 512) W = 1;
     // Past four warps only for large graphs, where each thread keeps at
     // least four vertex blocks (GB300, 32-64 chains: torus n = 20000 +15% at
     // P = 128 and +29% at P = 1 from four warps to eight, tree n = 10000 +2%
