@@ -272,6 +272,28 @@ def cpu_config1(target_s):
                       f"{el:.1f} s"}
 
 
+def gpu_config1(ctx):
+    """The plain-method small case on the GPU through the drop-in call: ER
+    n = 800, p = 0.06, +1 weights, 32 chains (raw seeds 0..31, t0 ladder),
+    the default schedule at its full 10^6 sweeps; chain-steps over the
+    call's device time, and over its wall time with host buffers."""
+    import rfmf_gb300 as R
+    g = R.erdos_renyi(800, 0.06, seed=0, name="er800_p0.06")
+    dg = R.DeviceGraph(ctx, g)
+    seeds = list(range(32))
+    init = np.stack([R.initial_spins(s, g.n) for s in seeds])
+    sol = [R.solver_seed(s) for s in seeds]
+    t0s = [LADDER[i % 8] for i in range(32)]
+    sweeps = 1_000_000
+    t = time.perf_counter()
+    res = R.anneal_gpu(ctx, dg, g.max_weighted_degree(), init, t0s, PHASES, [sweeps // 8] * 8, sol)
+    wall = time.perf_counter() - t
+    dg.close()
+    return {"value": 32 * sweeps / (res.kernel_ms / 1e3), "unit": "chain-steps/s",
+            "e2e_value": 32 * sweeps / wall, "best_cut": int(res.best_vals.max()),
+            "sample": "ER n=800 p=0.06 +1, 32 chains x 10^6 sweeps (phases 128..1), rfmf_anneal"}
+
+
 # --------------------------------------------------------------- GPU arm
 def gpu_arm(args, rank, world):
     import torch
@@ -385,6 +407,10 @@ def gpu_arm(args, rank, world):
         tt.append({"graph": g.name, "target_cut": target, "sweeps": (k_hit + 1) * per_step,
                    "seconds": sum(step_ms[:k_hit + 1]) / 1e3})
 
+    # the CPU-runnable small case, on the GPU (rank 0 of the default workload)
+    config1 = (gpu_config1(ctx) if rank == 0 and args.workload == WORKLOAD and not args.no_e2e
+               else None)
+
     # e2e through the drop-in call with host buffers
     e2e = None
     if not args.no_e2e:
@@ -470,6 +496,7 @@ def gpu_arm(args, rank, world):
         # of a multi-graph class is cut at phase boundaries)
         "gpu_launches": timed_launches,
         "e2e": e2e,
+        "config1_gpu": config1,
         "time_to_target": tt,
         "serving": serving,
         "serving_mixed_budgets": serving_mixed,
