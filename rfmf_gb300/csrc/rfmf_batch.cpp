@@ -378,13 +378,14 @@ int rebalance(rfmf_batch* b, uint32_t P, bool* changed = nullptr) {
 }
 
 // Warps per chain for phases of group count P in a batch whose width
-// follows the phase (one class, one graph, one-warp chains by rule, every
-// chain resident at two warps): two warps while the winners' rows hold at
-// least half as many entries as the graph has vertices (P >= 64), one
-// otherwise.  GB300, 1024 chains of ER n = 2000 d = 19, us per sweep at one
-// / two warps: P = 128 10.0 / 8.08, P = 64 6.11 / 5.43, P = 32 4.14 / 4.60,
-// P = 1 2.41 / 2.88; the 50x60 torus (512 row entries at P = 128) is
-// faster at one warp in every phase.
+// follows the phase (one class, one graph, the rule's width W, every chain
+// resident at 2W): 2W while the winners' rows hold at least half as many
+// entries as the graph has vertices (P >= 64), W otherwise.  GB300, us per
+// sweep at W / 2W: 1024 chains of ER n = 2000 d = 19 (W = 1) P = 128
+// 10.0 / 8.08, P = 64 6.11 / 5.43, P = 32 4.14 / 4.60, P = 1 2.41 / 2.88;
+// 32 chains of ER n = 800 d = 48 (W = 4) P = 128 5.56 / 4.39, P = 64
+// 3.92 / 3.49, P = 1 1.72 / 1.78; the 50x60 torus (512 row entries at
+// P = 128) is faster at one warp in every phase.
 bool wide_phase(const rfmf_graph* g, uint32_t P) {
     const double n = static_cast<double>(g->n);
     const double rows = std::min(static_cast<double>(P), n);
@@ -759,8 +760,8 @@ static int rfmf_batch_create_impl(rfmf_context* ctx, int64_t C, const rfmf_graph
     }
     b->cfg = c;
     for (BatchClass& k : b->cls) k.baseWarps = k.warps;
-    if (b->cls.size() == 1 && b->cls[0].graphs.size() == 1 && c.threads_per_chain == 0 && b->cls[0].warps == 1 &&
-        b->C * 2 <= int64_t(16) * ctx->sms) {
+    if (b->cls.size() == 1 && b->cls[0].graphs.size() == 1 && c.threads_per_chain == 0 &&
+        2 * b->cls[0].warps <= kMaxLatencyWarps && b->C * 2 * b->cls[0].warps <= int64_t(16) * ctx->sms) {
         for (uint32_t P : b->phaseP)
             b->phaseWarps = b->phaseWarps || (P && wide_phase(b->glist[b->cls[0].graphs[0]], P));
     }

@@ -228,3 +228,27 @@ def test_chain_width_follows_the_phase(rfmf, ctx, oracle):
     assert np.array_equal(np.stack(r["best_spins"]), ref["best_spins"])
     assert np.array_equal(r["cur_vals"], ref["cur_vals"])
     assert np.array_equal(r["best_vals"], ref["best_vals"])
+
+
+def test_four_warp_chains_widen_to_eight_in_row_heavy_phases(rfmf, ctx, oracle):
+    """32 chains of ER n = 800 p = 0.06 (four warps per chain by rule): eight
+    warps in the P = 128 phase, four after; every chain equals the oracle."""
+    g = rfmf.erdos_renyi(800, 0.06, seed=0)
+    C = 32
+    init, solver = chains_for(g, list(range(C)))
+    t0s = [35.0 + 15 * (i % 8) for i in range(C)]
+    phases, iters = [128, 1], [120, 120]
+    dg = rfmf.DeviceGraph(ctx, g)
+    b = rfmf.Batch(ctx, [dg] * C, t0s, solver, list(init), phases, iters)
+    b.run_timed(100)
+    wide = b.info()["threads_per_chain"]
+    b.run_timed(1000)
+    narrow = b.info()["threads_per_chain"]
+    r = b.read()
+    b.close()
+    dg.close()
+    assert (wide, narrow) == (256, 128), (wide, narrow)
+    ref = oracle.anneal(g, init, t0s, solver, phases, iters)
+    assert np.array_equal(np.stack(r["end_spins"]), ref["end_spins"])
+    assert np.array_equal(np.stack(r["best_spins"]), ref["best_spins"])
+    assert np.array_equal(r["best_vals"], ref["best_vals"])
