@@ -35,7 +35,9 @@ int rfmf_debug_fail_host_alloc(int64_t countdown);
  * CTAs, and level_ns[q * L + l - 1] the time per sweep of an item of graph q
  * at scheduler level l (warps on one SM scheduler, ceil(chains * warps / 4);
  * L = the level of a full CTA).  out_chains_per_item[q] receives graph q's
- * item size.  RFMF_ERR_CAPACITY when no sizes fit the slots. */
+ * item size: the one-round plan with the smallest makespan, or, when even
+ * the largest items need more than one round, sizes that shorten the
+ * queue's longest-first list schedule. */
 int rfmf_debug_plan_items(int ngraphs, const int64_t* chains, int max_chains_per_cta, int warps,
                           const double* level_ns, int64_t slots, int* out_chains_per_item);
 

@@ -25,10 +25,12 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <string>
 #include <memory>
 #include <new>
+#include <queue>
 #include <tuple>
 #include <vector>
 
@@ -198,17 +200,58 @@ int plan_class(rfmf_batch& b, BatchClass& k, const rfmf_launch_config& c, bool e
 }
 
 // Per-graph chains per item: graph q may use item sizes cand[q] (chain
-// count, item time per sweep; time non-decreasing in chain count), and all
-// items must fit `slots` resident CTAs.  The smallest makespan tau wins, each
-// graph taking its largest size whose time is <= tau.  False (kg untouched)
-// when nothing fits.
+// count, item time per sweep; ascending in both, each the largest count of
+// its scheduler level), over `slots` resident CTAs that take items from the
+// queue in order, longest first.
+//
+// When every item fits one round of the slots, the smallest makespan tau
+// wins, each graph taking its largest size whose time is <= tau.  When even
+// the largest sizes need more than one round, the makespan is that of the
+// queue's longest-first list schedule, and sizes are lowered one graph and
+// one level at a time while that shortens it (GB300, large sparse shapes,
+// 768 chains of four warps on 152 CTAs: 7.85e7 -> 8.33e7 chain-steps/s).
+// That model holds for a class alone on the GPU; classes that share the SMs
+// (`rounds` false) keep their sizes instead (the 512-graph mix in six
+// classes lost 5% under it).  False (kg untouched) when nothing is planned.
 struct ItemCand {
     int K;
     double ns;
 };
+
+// The list-schedule makespan of sizes idx[q] (indices into cand[q]): items
+// of the chosen size plus one remainder item per graph, longest first, each
+// to the slot that frees first.
+double list_makespan(const std::vector<std::vector<ItemCand>>& cand, const std::vector<int64_t>& chains,
+                     const std::vector<size_t>& idx, int64_t slots) {
+    std::vector<double> items;
+    for (size_t q = 0; q < cand.size(); ++q) {
+        const ItemCand& c = cand[q][idx[q]];
+        const int64_t full = chains[q] / c.K, rest = chains[q] % c.K;
+        items.insert(items.end(), static_cast<size_t>(full), c.ns);
+        if (rest) {
+            size_t r = 0;
+            while (cand[q][r].K < rest) ++r;   // the level of a partial item
+            items.push_back(cand[q][r].ns);
+        }
+    }
+    std::sort(items.begin(), items.end(), std::greater<double>());
+    const size_t S = static_cast<size_t>(std::max<int64_t>(1, std::min<int64_t>(slots, static_cast<int64_t>(items.size()))));
+    std::priority_queue<double, std::vector<double>, std::greater<double>> freeAt;
+    for (size_t i = 0; i < S; ++i) freeAt.push(0.0);
+    double span = 0.0;
+    for (double t : items) {
+        const double f = freeAt.top() + t;
+        freeAt.pop();
+        freeAt.push(f);
+        span = std::max(span, f);
+    }
+    return span;
+}
+
 bool balance_items(const std::vector<std::vector<ItemCand>>& cand, const std::vector<int64_t>& chains,
-                   int64_t slots, std::vector<int>& kg) {
+                   int64_t slots, std::vector<int>& kg, bool rounds = true) {
     const size_t G = cand.size();
+    if (G == 0) return false;
     std::vector<double> taus;
     for (const auto& cq : cand)
         for (const ItemCand& c : cq) taus.push_back(c.ns);
@@ -231,8 +274,35 @@ bool balance_items(const std::vector<std::vector<ItemCand>>& cand, const std::ve
         const size_t mid = (lo + hi) / 2;
         if (pick(taus[mid], trial)) hi = mid; else lo = mid + 1;
     }
-    if (lo == taus.size() || !pick(taus[lo], trial)) return false;
-    kg = trial;
+    if (lo < taus.size() && pick(taus[lo], trial)) {
+        kg = trial;
+        return true;
+    }
+    if (!rounds) return false;
+    // More than one round: descend from the largest sizes (at most 2000
+    // schedule evaluations, a few hundred ms for the largest classes).
+    std::vector<size_t> idx(G);
+    for (size_t q = 0; q < G; ++q) idx[q] = cand[q].size() - 1;
+    double best = list_makespan(cand, chains, idx, slots);
+    int evals = 1;
+    for (bool improved = true; improved && evals < 2000;) {
+        improved = false;
+        size_t bestQ = G;
+        for (size_t q = 0; q < G && evals < 2000; ++q) {
+            if (idx[q] == 0) continue;
+            --idx[q];
+            const double m = list_makespan(cand, chains, idx, slots);
+            ++evals;
+            ++idx[q];
+            if (m < best * (1.0 - 1e-9)) { best = m; bestQ = q; }
+        }
+        if (bestQ < G) {
+            --idx[bestQ];
+            improved = true;
+        }
+    }
+    kg.assign(G, 0);
+    for (size_t q = 0; q < G; ++q) kg[q] = cand[q][idx[q]].K;
     return true;
 }
 
@@ -271,7 +341,7 @@ bool plan_balanced(const rfmf_batch& b, const BatchClass& k, uint32_t P, std::ve
             cand[q].push_back({K, item_cost(b, k, q, P, sched_level(K, k.warps), learned)});
         }
     }
-    return balance_items(cand, chains, static_cast<int64_t>(k.occ) * b.ctx->sms, kg);
+    return balance_items(cand, chains, static_cast<int64_t>(k.occ) * b.ctx->sms, kg, b.cls.size() == 1);
 }
 
 // Items: graphs in decreasing per-item cost, each graph's chains in groups of

@@ -5,10 +5,8 @@ torus and ER n = 2000 d = 19, 1024 one-warp chains each, 150 resident
 CTAs of up to 16 chains), it must pick the sizes that were fastest when
 forced: 16 torus / 12 ER chains per item at P = 128 (11.06 us per sweep
 against 12.2-12.4 for every other fitting split) and 12 / 16 at P = 1
-(3.74 against 4.52)."""
-import pytest
-
-from rfmf_gb300 import RfmfError
+(3.74 against 4.52).  When even the largest items need more than one round
+of the CTAs, it minimises the queue's longest-first list schedule."""
 
 
 def _levels(l3, l4):
@@ -49,6 +47,16 @@ def test_level_boundaries_follow_warps_per_chain(rfmf):
     assert kg == [2, 2]
 
 
-def test_no_fit_is_a_capacity_error(rfmf):
-    with pytest.raises(RfmfError):
-        rfmf.debug_plan_items([5000, 5000], 16, 1, [_levels(1, 2)] * 2, 100)
+def test_more_than_one_round_minimises_the_list_schedule(rfmf):
+    # 768 four-warp chains of three large sparse graphs on 152 CTAs of at
+    # most four chains (levels 1..4 = 1..4 chains): the largest items need
+    # 192 > 152 slots.  Items of 6.8 / 4.2 / 2.94 us per sweep at level 4
+    # (scaled (L + 3) / 7 below) leave 16 cheap items for a second round on
+    # the tree's slots (makespan 7.14); three-chain tree items shorten the
+    # schedule to the torus items' 6.8, which bounds it.
+    lv = lambda t: [t * (L + 3) / 7 for L in (1, 2, 3, 4)]
+    kg = rfmf.debug_plan_items([256, 256, 256], 4, 4, [lv(6.8), lv(4.2), lv(2.94)], 152)
+    assert kg == [4, 3, 4], kg
+    # deep queues: smaller items cost more per chain, so full ones stay
+    kg = rfmf.debug_plan_items([5000, 5000], 16, 1, [_levels(1.0, 1.2)] * 2, 100)
+    assert kg == [16, 16], kg
