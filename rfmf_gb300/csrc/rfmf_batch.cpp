@@ -330,7 +330,12 @@ double item_cost(const rfmf_batch& b, const BatchClass& k, size_t q, uint32_t P,
 // the split).
 bool plan_balanced(const rfmf_batch& b, const BatchClass& k, uint32_t P, std::vector<int>& kg) {
     const size_t G = k.graphs.size();
-    if (G < 2) return false;
+    const bool alone = b.cls.size() == 1;
+    const int64_t slots = static_cast<int64_t>(k.occ) * b.ctx->sms;
+    // One graph: its uniform items are right unless even full ones need
+    // more than one round (then the list schedule decides, as below).
+    if (G == 0 || (G == 1 && !(alone && (static_cast<int64_t>(k.chainsOf[0].size()) + k.K - 1) / k.K > slots)))
+        return false;
     const bool learned = class_learned(b, k, P);
     std::vector<std::vector<ItemCand>> cand(G);
     std::vector<int64_t> chains(G);
@@ -341,7 +346,7 @@ bool plan_balanced(const rfmf_batch& b, const BatchClass& k, uint32_t P, std::ve
             cand[q].push_back({K, item_cost(b, k, q, P, sched_level(K, k.warps), learned)});
         }
     }
-    return balance_items(cand, chains, static_cast<int64_t>(k.occ) * b.ctx->sms, kg, b.cls.size() == 1);
+    return balance_items(cand, chains, slots, kg, alone);
 }
 
 // Items: graphs in decreasing per-item cost, each graph's chains in groups of
@@ -424,15 +429,15 @@ uint32_t phase_at(const rfmf_batch& b, uint64_t sweep, uint64_t* end) {
     return last;
 }
 
-// Size the work items of multi-graph classes for phases of group count P
-// from the costs learned so far (re-planned before every launch: costs
-// keep arriving, and planning is a few microseconds per graph); uploaded
-// only when the per-graph item sizes change (stream-ordered after older
+// Size the work items of classes for phases of group count P (multi-graph
+// classes, and a lone class whose items need more than one round) from the
+// costs learned so far (re-planned before every launch: costs keep
+// arriving, and planning is a few microseconds per graph); uploaded only
+// when the per-graph item sizes change (stream-ordered after older
 // launches).  *changed (optional) tells whether any class's items did.
 int rebalance(rfmf_batch* b, uint32_t P, bool* changed = nullptr) {
     if (changed) *changed = false;
     for (BatchClass& k : b->cls) {
-        if (k.graphs.size() < 2) continue;
         std::vector<int> kg;
         if (!plan_balanced(*b, k, P, kg)) continue;
         const bool differ = !k.balanced || kg != k.Kg;

@@ -60,3 +60,11 @@ def test_more_than_one_round_minimises_the_list_schedule(rfmf):
     # deep queues: smaller items cost more per chain, so full ones stay
     kg = rfmf.debug_plan_items([5000, 5000], 16, 1, [_levels(1.0, 1.2)] * 2, 100)
     assert kg == [16, 16], kg
+
+
+def test_one_graph_past_one_round_drops_a_level(rfmf):
+    # 3000 one-warp chains of one graph on 152 CTAs of 16: full items take
+    # two rounds (188 items); twelve-chain items (level 3, 250 items) also
+    # take two, each round 6/7 as long
+    kg = rfmf.debug_plan_items([3000], 16, 1, [_levels(6.0, 7.0)], 152)
+    assert kg == [12], kg
