@@ -252,3 +252,29 @@ def test_four_warp_chains_widen_to_eight_in_row_heavy_phases(rfmf, ctx, oracle):
     assert np.array_equal(np.stack(r["end_spins"]), ref["end_spins"])
     assert np.array_equal(np.stack(r["best_spins"]), ref["best_spins"])
     assert np.array_equal(r["best_vals"], ref["best_vals"])
+
+
+def test_one_graph_past_one_round_of_ctas(rfmf, ctx, oracle):
+    """More one-warp chains of one graph than one round of 16-chain CTAs
+    holds (2600 > 16 x 152): the planner sizes the items for the queue's
+    list schedule (smaller items than 16); every chain equals the oracle."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    g = rfmf.erdos_renyi(300, 0.04, signed=True, seed=12)
+    C = 16 * sms + 168
+    init, solver = chains_for(g, list(range(8000, 8000 + C)))
+    t0s = [35.0 + 15 * (i % 8) for i in range(C)]
+    phases, iters = [32, 1], [100, 100]
+    dg = rfmf.DeviceGraph(ctx, g)
+    b = rfmf.Batch(ctx, [dg] * C, t0s, solver, list(init), phases, iters)
+    assert b.info()["threads_per_chain"] == 32
+    b.run(200)
+    info = b.info()
+    r = b.read()
+    b.close()
+    dg.close()
+    assert info["items"] > -(-C // 16), info
+    ref = oracle.anneal(g, init, t0s, solver, phases, iters)
+    assert np.array_equal(np.stack(r["end_spins"]), ref["end_spins"])
+    assert np.array_equal(np.stack(r["best_spins"]), ref["best_spins"])
+    assert np.array_equal(r["best_vals"], ref["best_vals"])
